@@ -1,0 +1,852 @@
+/*
+ * CPU restatement of the reference BayesianGroupTesting lattice hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg load it to check and
+ * to time the CUDA provider.  Nothing in the shipped GPU path links it, calls
+ * it or falls back to it.
+ *
+ * Every function restates one piece of the reference CPU provider (paths
+ * relative to the reference repository) with the same operation order, so
+ * that, compiled with IEEE semantics (no -ffast-math, -ffp-contract=off), it
+ * reproduces the reference built the same way bit for bit.  That property is
+ * pinned by tests/test_oracle.py against the reference library itself
+ * (oracle/_ref, built by oracle/ref/Makefile where the reference sources are
+ * present) and against the golden vectors in tests/golden/.
+ *
+ * Conventions (reference facts): a state is a 32-bit word, atom index =
+ * variant * subjects + subject; bit set = negative (healthy); pi0[i] is the
+ * prevalence P(atom i positive).  Lattice "dilution" flag: 0 = replicated
+ * non-dilution, 1 = replicated dilution.  Selector ids follow bgt::SelectorType:
+ * 0 = auto, 1 = Op-BHA, 2 = Op-BBPA.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "bgt_session_rng.h"
+
+#define ORC_EXPORT __attribute__((visibility("default")))
+
+static int orc_popcount(uint32_t v) { return __builtin_popcount(v); }
+
+/* ------------------------------------------------------------------ model */
+
+/* DilutionTable(subjects, alpha, h), src/core/model/dilution.cpp:44-64.
+ * Row-major n x (n+1); row L-1 holds pool size L, column r = positives in pool. */
+ORC_EXPORT void orc_dilution_table(int n, double alpha, double h, double *out)
+{
+	memset(out, 0, sizeof(double) * (size_t)n * (size_t)(n + 1));
+	for (int rk = 1; rk <= n; rk++)
+	{
+		double *row = out + (size_t)(rk - 1) * (size_t)(n + 1);
+		row[0] = alpha;
+		for (int r = 1; r <= rk; r++)
+		{
+			const int k = rk - r;
+			row[r] = 1 - alpha * r / (k * h + r);
+		}
+	}
+}
+
+/* ReplicatedNonDilutionLattice::response_prob,
+ * src/core/model/replicated_lattice.cpp:8-14, and
+ * ReplicatedDilutionLattice::response_prob, :17-28.  `subjects` is the
+ * lattice's current subject count; `dil` is the full table of the original
+ * subject count with row stride `dil_stride`.  An empty dilution pool (the
+ * reference indexes row -1 there) uses the alpha column, as the session
+ * sampler does. */
+ORC_EXPORT double orc_response_prob(int dilution, int subjects, int variants, uint32_t e, uint32_t r, uint32_t s,
+									const double *dil, int dil_stride)
+{
+	double ret = 1.0;
+	if (!dilution)
+	{
+		const double negative_response = BGT_NON_DILUTION_NEGATIVE;
+		for (int v = 0; v < variants; v++)
+		{
+			const uint32_t shifted = (uint32_t)((uint64_t)s >> (v * subjects));
+			const int bit = (r & (1u << v)) != 0;
+			ret *= ((e & shifted) == e) ? (bit == 0 ? (1.0 - negative_response) : negative_response)
+										: (bit == 0 ? negative_response : (1.0 - negative_response));
+		}
+		return ret;
+	}
+	const int length = orc_popcount(e);
+	for (int v = 0; v < variants; v++)
+	{
+		const uint32_t shifted = (uint32_t)((uint64_t)s >> (v * subjects));
+		const int col = length - orc_popcount(e & shifted);
+		const double p = length == 0 ? dil[0] : dil[(size_t)(length - 1) * (size_t)dil_stride + (size_t)col];
+		ret *= (r & (1u << v)) != 0 ? p : 1.0 - p;
+	}
+	return ret;
+}
+
+/* Lattice::prior_prob, src/core/model/lattice_base.cpp:197-208. */
+ORC_EXPORT double orc_prior_prob(int atoms, const double *pi0, uint32_t state)
+{
+	double prob = 1.0;
+	for (int i = 0; i < atoms; i++)
+	{
+		if ((state & (1u << i)) == 0)
+			prob *= pi0[i];
+		else
+			prob *= (1.0 - pi0[i]);
+	}
+	return prob;
+}
+
+/* Lattice::prior_probs, lattice_base.cpp:184-195. */
+ORC_EXPORT void orc_prior(int atoms, const double *pi0, double *out)
+{
+	const size_t count = (size_t)1 << atoms;
+	for (size_t i = 0; i < count; i++)
+		out[i] = orc_prior_prob(atoms, pi0, (uint32_t)i);
+}
+
+/* Lattice::update_probs (multiply by 1/denominator), lattice_base.cpp:210-228,
+ * when in_place == 0; Lattice::update_probs_in_place (divide by the
+ * denominator), :230-244, otherwise.  Writes `out` (may alias `post`).
+ * Returns the denominator. */
+ORC_EXPORT double orc_update(int dilution, int subjects, int variants, const double *post, double *out, uint32_t e,
+							 uint32_t r, const double *dil, int dil_stride, int in_place)
+{
+	const size_t count = (size_t)1 << (subjects * variants);
+	double denominator = 0.0;
+	for (size_t i = 0; i < count; i++)
+	{
+		out[i] = post[i] * orc_response_prob(dilution, subjects, variants, e, r, (uint32_t)i, dil, dil_stride);
+		denominator += out[i];
+	}
+	if (in_place)
+	{
+		for (size_t i = 0; i < count; i++)
+			out[i] = out[i] / denominator;
+	}
+	else
+	{
+		const double inv = 1.0 / denominator;
+		for (size_t i = 0; i < count; i++)
+			out[i] = out[i] * inv;
+	}
+	return denominator;
+}
+
+/* compute_atom_masses, lattice_base.cpp:25-41 (state-major order). */
+ORC_EXPORT void orc_atom_masses(const double *post, int atoms, double *masses)
+{
+	const size_t count = (size_t)1 << atoms;
+	for (int a = 0; a < atoms; a++)
+		masses[a] = 0.0;
+	for (size_t s = 0; s < count; s++)
+	{
+		const double p = post[s];
+		for (int a = 0; a < atoms; a++)
+			if ((uint32_t)s & (1u << a))
+				masses[a] += p;
+	}
+}
+
+/* Lattice::update_metadata, lattice_base.cpp:246-264.  Masks are in/out. */
+ORC_EXPORT void orc_classify_masses(const double *masses, int atoms, double up, double lo, uint32_t *pos, uint32_t *neg)
+{
+	for (int i = 0; i < atoms; i++)
+	{
+		const uint32_t placement = 1u << i;
+		if ((*pos | *neg) & placement)
+			continue;
+		const double m = masses[i];
+		if (m < lo)
+			*pos |= placement;
+		else if (m > (1 - up))
+			*neg |= placement;
+	}
+}
+
+ORC_EXPORT void orc_classify(const double *post, int atoms, double up, double lo, uint32_t *pos, uint32_t *neg)
+{
+	double masses[32];
+	orc_atom_masses(post, atoms, masses);
+	orc_classify_masses(masses, atoms, up, lo, pos, neg);
+}
+
+/* Lattice::get_prob_mass (active generation), lattice_base.cpp:319-351. */
+ORC_EXPORT double orc_upset_mass(const double *post, int atoms, uint32_t state)
+{
+	uint32_t add_index[32];
+	int n = 0;
+	for (int i = 0; i < atoms; i++)
+		if (!(state & (1u << i)))
+			add_index[n++] = 1u << i;
+	double ret = 0.0;
+	const uint64_t pow_set = (uint64_t)1 << n;
+	for (uint64_t i = 0; i < pow_set; i++)
+	{
+		uint32_t temp = state;
+		for (int j = 0; j < n; j++)
+			if (i & ((uint64_t)1 << j))
+				temp |= add_index[j];
+		ret += post[temp];
+	}
+	return ret;
+}
+
+/* -------------------------------------------------------------- selectors */
+
+/* subset_zeta_transform, src/kernels/cpu/bbpa.cpp:497-512: ascending bits,
+ * a[base+off] += a[base+off+bit]. */
+ORC_EXPORT void orc_zeta(double *a, int bits)
+{
+	const size_t count = (size_t)1 << bits;
+	for (int subject = 0; subject < bits; subject++)
+	{
+		const size_t bit = (size_t)1 << subject;
+		const size_t step = bit << 1;
+		for (size_t base = 0; base < count; base += step)
+			for (size_t off = 0; off < bit; off++)
+				a[base + off] += a[base + off + bit];
+	}
+}
+
+/* Op-BHA, bbpa.cpp:902-916 with best_op_bha_candidate :537-551.
+ * `scratch` holds 2^subjects doubles (the upset masses on return). */
+ORC_EXPORT uint32_t orc_op_bha(const double *post, int subjects, double *scratch)
+{
+	const size_t count = (size_t)1 << subjects;
+	for (size_t s = 0; s < count; s++)
+		scratch[s] = post[s];
+	orc_zeta(scratch, subjects);
+	uint32_t candidate = 0;
+	double best = 2.0;
+	for (size_t e = 0; e < count; e++)
+	{
+		const double distance = fabs(scratch[e] - 0.5);
+		if (distance < best)
+		{
+			best = distance;
+			candidate = (uint32_t)e;
+		}
+	}
+	return candidate;
+}
+
+static int orc_better(double score, uint32_t e, double best, uint32_t best_e)
+{
+	return score < best || (score == best && e < best_e);
+}
+
+/* Lattice::BBPA_serial, bbpa.cpp:950-970, with the binary path
+ * (build_binary_positive_mask_masses :79-96, best_binary_partition_candidate
+ * :201-220), the two-variant path (build_two_variant_intersection_masses
+ * :113-141, best_two_variant_partition_candidate :332-365) and the generic
+ * path (build_variant_subset_intersection_masses :237-285,
+ * transform_variant_subset_masses :292-300,
+ * best_multinomial_partition_candidate :416-460).  `table` holds
+ * 2^variants * 2^subjects doubles (feature tables on return); `best_score`
+ * receives the winning score when non-null. */
+ORC_EXPORT uint32_t orc_bbpa(const double *post, int subjects, int variants, double target, double *table,
+							 double *best_score)
+{
+	const size_t E = (size_t)1 << subjects;
+	const int R = 1 << variants;
+	const size_t states = (size_t)1 << (subjects * variants);
+	const uint32_t mask = (uint32_t)(E - 1);
+	memset(table, 0, sizeof(double) * E * (size_t)R);
+	double best = 2.0;
+	uint32_t cand = 0xFFFFFFFFu;
+	if (variants == 1)
+	{
+		double total = 0.0;
+		for (size_t s = 0; s < states; s++)
+		{
+			table[(uint32_t)s & mask] += post[s];
+			total += post[s];
+		}
+		orc_zeta(table, subjects);
+		for (size_t e = 0; e < E; e++)
+		{
+			const double positive = table[e];
+			const double negative = total - positive;
+			const double score = fabs(positive - target) + fabs(negative - target);
+			if (orc_better(score, (uint32_t)e, best, cand))
+			{
+				best = score;
+				cand = (uint32_t)e;
+			}
+		}
+	}
+	else if (variants == 2)
+	{
+		double *v0 = table + E, *v1 = table + 2 * E, *both = table + 3 * E;
+		double total = 0.0;
+		for (size_t s = 0; s < states; s++)
+		{
+			const uint32_t m0 = (uint32_t)s & mask;
+			const uint32_t m1 = ((uint32_t)s >> subjects) & mask;
+			const double mass = post[s];
+			v0[m0] += mass;
+			v1[m1] += mass;
+			both[m0 & m1] += mass;
+			total += mass;
+		}
+		table[0] = total;
+		for (int b = 1; b < 4; b++)
+			orc_zeta(table + (size_t)b * E, subjects);
+		for (size_t e = 0; e < E; e++)
+		{
+			const double p0 = v0[e], p1 = v1[e], pb = both[e];
+			const double r0 = pb;
+			const double r1 = p1 - pb;
+			const double r2 = p0 - pb;
+			const double r3 = total - p0 - p1 + pb;
+			const double score = fabs(r0 - target) + fabs(r1 - target) + fabs(r2 - target) + fabs(r3 - target);
+			if (orc_better(score, (uint32_t)e, best, cand))
+			{
+				best = score;
+				cand = (uint32_t)e;
+			}
+		}
+	}
+	else
+	{
+		uint32_t vm[32], inter[1 << 10];
+		double total = 0.0;
+		for (size_t s = 0; s < states; s++)
+		{
+			const double mass = post[s];
+			for (int v = 0; v < variants; v++)
+				vm[v] = (uint32_t)(((uint64_t)s >> (v * subjects)) & mask);
+			inter[0] = mask;
+			for (int subset = 1; subset < R; subset++)
+			{
+				const int low = subset & -subset;
+				const int v = __builtin_ctz((unsigned)low);
+				const uint32_t x = inter[subset ^ low] & vm[v];
+				inter[subset] = x;
+				table[(size_t)subset * E + x] += mass;
+			}
+			total += mass;
+		}
+		table[0] = total;
+		for (int b = 1; b < R; b++)
+			orc_zeta(table + (size_t)b * E, subjects);
+		const int all = R - 1;
+		for (size_t e = 0; e < E; e++)
+		{
+			double score = 0.0;
+			for (int response = 0; response < R; response++)
+			{
+				const int positive = (~response) & all;
+				const int missing = response;
+				double exact = 0.0;
+				for (int extra = missing;; extra = (extra - 1) & missing)
+				{
+					const int fs = positive | extra;
+					const double feature = fs == 0 ? total : table[(size_t)fs * E + e];
+					if ((orc_popcount((uint32_t)extra) & 1) == 0)
+						exact += feature;
+					else
+						exact -= feature;
+					if (extra == 0)
+						break;
+				}
+				score += fabs(exact - target);
+			}
+			if (orc_better(score, (uint32_t)e, best, cand))
+			{
+				best = score;
+				cand = (uint32_t)e;
+			}
+		}
+	}
+	if (best_score)
+		*best_score = best;
+	return cand;
+}
+
+/* resolve_selector, src/runtime/simulation_helpers.cpp:40-45, and
+ * Lattice::select_experiment, bbpa.cpp:861-871 (target 1/2^k,
+ * selector_target_mass :575-587).  Returns 0xFFFFFFFF for Op-BHA with k > 1
+ * (the reference throws). `scratch` holds 2^variants * 2^subjects doubles. */
+ORC_EXPORT uint32_t orc_select(const double *post, int subjects, int variants, int selector, double *scratch)
+{
+	const int resolved = selector == 0 ? (variants == 1 ? 1 : 2) : selector;
+	if (resolved == 1)
+	{
+		if (variants != 1)
+			return 0xFFFFFFFFu;
+		return orc_op_bha(post, subjects, scratch);
+	}
+	return orc_bbpa(post, subjects, variants, 1.0 / (double)(1 << variants), scratch, NULL);
+}
+
+/* ---------------------------------------------------------------- session */
+
+/* One adaptive session in the bgt::Lattice call order
+ * (src/core/lattice_api.cpp:108-178): select -> sampled response ->
+ * update_probs_in_place -> update_metadata, `stages` times.  `post` holds the
+ * prior on entry (or is built from pi0 when `post_in` is null) and the final
+ * posterior on return. */
+ORC_EXPORT int orc_session(int dilution, int subjects, int variants, const double *pi0, int selector, double alpha,
+						   double h, double up, double lo, int stages, uint64_t seed, uint64_t session,
+						   uint32_t true_state, uint32_t *experiments, uint32_t *responses, uint32_t *pos_masks,
+						   uint32_t *neg_masks, double *post)
+{
+	const int atoms = subjects * variants;
+	const size_t count = (size_t)1 << atoms;
+	double *scratch = (double *)malloc(sizeof(double) * ((size_t)1 << subjects) * (size_t)(1 << variants));
+	double *dil = (double *)malloc(sizeof(double) * (size_t)subjects * (size_t)(subjects + 1));
+	if (!scratch || !dil)
+	{
+		free(scratch);
+		free(dil);
+		return 4;
+	}
+	orc_dilution_table(subjects, alpha, h, dil);
+	orc_prior(atoms, pi0, post);
+	uint32_t pos = 0, neg = 0;
+	for (int stage = 0; stage < stages; stage++)
+	{
+		const uint32_t e = orc_select(post, subjects, variants, selector, scratch);
+		const uint32_t r = bgt_session_sample_response(dilution, subjects, variants, e, true_state, alpha, h, seed,
+													   session, (uint32_t)stage);
+		orc_update(dilution, subjects, variants, post, post, e, r, dil, subjects + 1, 1);
+		orc_classify(post, atoms, up, lo, &pos, &neg);
+		experiments[stage] = e;
+		responses[stage] = r;
+		pos_masks[stage] = pos;
+		neg_masks[stage] = neg;
+	}
+	(void)count;
+	free(scratch);
+	free(dil);
+	return 0;
+}
+
+/* ------------------------------------------------------------------- tree */
+
+typedef struct OrcNode
+{
+	uint32_t ex, res;
+	int stage;
+	double branch_prob;
+	uint32_t pos, neg;
+	int first_child; /* index into the node array, -1 for a leaf */
+} OrcNode;
+
+typedef struct OrcLattice
+{
+	int curr_subjs;
+	uint32_t pos, neg, clas_subjs;
+	double *post;
+} OrcLattice;
+
+typedef struct OrcTree
+{
+	int orig_subjs, variants, depth, selector, dilution;
+	double up, lo;
+	const double *dil;
+	OrcNode *nodes;
+	int count, capacity;
+	double *scratch;
+	int failed;
+} OrcTree;
+
+static int orc_is_classified(const OrcTree *t, uint32_t pos, uint32_t neg)
+{
+	return orc_popcount(pos | neg) == t->orig_subjs * t->variants;
+}
+
+/* make_shrink_plan, src/core/model/shrink_plan.cpp:124-177, reduced to what
+ * the tree needs: original -> current atom positions, the removable current
+ * atoms (curr_shrinkable_atoms :31-54) and the newly classified subjects
+ * (update_clas_subj :56-76). */
+typedef struct OrcPlan
+{
+	int orig_to_curr[32];
+	uint32_t removable;
+	uint32_t new_clas_subjs;
+	int new_curr_subjs;
+} OrcPlan;
+
+static OrcPlan orc_make_plan(int orig, int curr, int variants, uint32_t classified_atoms, uint32_t clas_subjs)
+{
+	OrcPlan plan;
+	int subject_to_curr[32];
+	int next = 0;
+	for (int i = 0; i < 32; i++)
+		plan.orig_to_curr[i] = -1;
+	for (int s = 0; s < orig; s++)
+		subject_to_curr[s] = (clas_subjs & (1u << s)) ? -1 : next++;
+	uint32_t curr_classified = 0;
+	for (int s = 0; s < orig; s++)
+	{
+		const int p = subject_to_curr[s];
+		if (p < 0)
+			continue;
+		for (int v = 0; v < variants; v++)
+		{
+			const int oa = v * orig + s, ca = v * curr + p;
+			plan.orig_to_curr[oa] = ca;
+			if (classified_atoms & (1u << oa))
+				curr_classified |= 1u << ca;
+		}
+	}
+	plan.removable = 0;
+	for (int i = 0; i < curr; i++)
+	{
+		int all = 1;
+		for (int v = 0; v < variants; v++)
+			if (!(curr_classified & (1u << (v * curr + i))))
+				all = 0;
+		if (all)
+			for (int v = 0; v < variants; v++)
+				plan.removable |= 1u << (v * curr + i);
+	}
+	plan.new_clas_subjs = 0;
+	for (int s = 0; s < orig; s++)
+	{
+		int all = 1;
+		for (int v = 0; v < variants; v++)
+			if (!(classified_atoms & (1u << (v * orig + s))))
+				all = 0;
+		if (all)
+			plan.new_clas_subjs |= 1u << s;
+	}
+	plan.new_curr_subjs = orig - orc_popcount(plan.new_clas_subjs);
+	return plan;
+}
+
+/* project_posterior, include/bgt/detail/model/shrink.hpp:249-265 (ascending
+ * base states, each summing its reduced states in ascending order). */
+static double *orc_project(const double *src, int source_atoms, uint32_t removable)
+{
+	uint32_t base_masks[32], reduced_masks[32];
+	int nb = 0, nr = 0;
+	for (int a = 0; a < source_atoms; a++)
+	{
+		if (removable & (1u << a))
+			reduced_masks[nr++] = 1u << a;
+		else
+			base_masks[nb++] = 1u << a;
+	}
+	double *dst = (double *)malloc(sizeof(double) * ((size_t)1 << nb));
+	if (!dst)
+		return NULL;
+	for (size_t b = 0; b < ((size_t)1 << nb); b++)
+	{
+		uint32_t base_state = 0;
+		for (int i = 0; i < nb; i++)
+			if (b & ((size_t)1 << i))
+				base_state |= base_masks[i];
+		double sum = 0.0;
+		for (size_t r = 0; r < ((size_t)1 << nr); r++)
+		{
+			uint32_t reduced_state = 0;
+			for (int i = 0; i < nr; i++)
+				if (r & ((size_t)1 << i))
+					reduced_state |= reduced_masks[i];
+			sum += src[base_state | reduced_state];
+		}
+		dst[b] = sum;
+	}
+	return dst;
+}
+
+/* Lattice::update_metadata_with_shrinking, lattice_base.cpp:266-305, with
+ * apply_shrink_plan :307-316. */
+static int orc_update_with_shrinking(const OrcTree *t, OrcLattice *l)
+{
+	const int orig = t->orig_subjs, variants = t->variants;
+	const uint32_t clas_atoms = l->pos | l->neg;
+	const OrcPlan old_plan = orc_make_plan(orig, l->curr_subjs, variants, clas_atoms, l->clas_subjs);
+	double masses[32];
+	orc_atom_masses(l->post, l->curr_subjs * variants, masses);
+	uint32_t new_pos = 0, new_neg = 0;
+	for (int i = 0; i < orig * variants; i++)
+	{
+		const uint32_t bit = 1u << i;
+		if (clas_atoms & bit)
+			continue;
+		const int cur = old_plan.orig_to_curr[i];
+		if (cur < 0)
+			continue;
+		const double m = masses[cur];
+		if (m < t->lo)
+			new_pos |= bit;
+		else if (m > (1 - t->up))
+			new_neg |= bit;
+	}
+	l->pos |= new_pos;
+	l->neg |= new_neg;
+	const OrcPlan plan = orc_make_plan(orig, l->curr_subjs, variants, l->pos | l->neg, l->clas_subjs);
+	if (plan.removable != 0)
+	{
+		double *projected = orc_project(l->post, l->curr_subjs * variants, plan.removable);
+		if (!projected)
+			return 0;
+		free(l->post);
+		l->post = projected;
+		l->clas_subjs = plan.new_clas_subjs;
+		l->curr_subjs = plan.new_curr_subjs;
+	}
+	return 1;
+}
+
+/* Tree::true_ex, src/core/tree/tree.cpp:55-68. */
+static uint32_t orc_true_ex(int orig_subjs, uint32_t clas_subjs, uint32_t halving)
+{
+	uint32_t ret = 0, pos = 0;
+	for (int i = 0; i < orig_subjs; i++)
+	{
+		if (!(clas_subjs & (1u << i)))
+		{
+			if (halving & (1u << pos))
+				ret |= 1u << i;
+			++pos;
+		}
+	}
+	return ret;
+}
+
+static int orc_new_node(OrcTree *t)
+{
+	if (t->count == t->capacity)
+	{
+		const int cap = t->capacity ? t->capacity * 2 : 64;
+		OrcNode *nodes = (OrcNode *)realloc(t->nodes, sizeof(OrcNode) * (size_t)cap);
+		if (!nodes)
+		{
+			t->failed = 1;
+			return -1;
+		}
+		t->nodes = nodes;
+		t->capacity = cap;
+	}
+	return t->count++;
+}
+
+/* LocalTree::LocalTree, src/core/tree/global_tree_intra.cpp:8-40.  Takes
+ * ownership of l->post.  Children of a node occupy consecutive slots. */
+static void orc_build(OrcTree *t, int node, OrcLattice *l)
+{
+	OrcNode *nd = &t->nodes[node];
+	nd->pos = l->pos;
+	nd->neg = l->neg;
+	nd->first_child = -1;
+	if (orc_is_classified(t, l->pos, l->neg) || nd->stage >= t->depth)
+	{
+		free(l->post);
+		l->post = NULL;
+		return;
+	}
+	const int R = 1 << t->variants;
+	const uint32_t bbpa = orc_select(l->post, l->curr_subjs, t->variants, t->selector, t->scratch);
+	const uint32_t ex = orc_true_ex(t->orig_subjs, l->clas_subjs, bbpa);
+	const int stage = nd->stage;
+	int first = -1;
+	for (int re = 0; re < R; re++)
+	{
+		const int c = orc_new_node(t);
+		if (c < 0)
+			return;
+		if (re == 0)
+			first = c;
+	}
+	t->nodes[node].first_child = first;
+	const size_t count = (size_t)1 << (l->curr_subjs * t->variants);
+	for (int re = 0; re < R; re++)
+	{
+		OrcLattice child = *l;
+		if (re != R - 1)
+		{
+			child.post = (double *)malloc(sizeof(double) * count);
+			if (!child.post)
+			{
+				t->failed = 1;
+				return;
+			}
+			orc_update(t->dilution, l->curr_subjs, t->variants, l->post, child.post, bbpa, (uint32_t)re, t->dil,
+					   t->orig_subjs + 1, 0);
+		}
+		else
+		{
+			child.post = l->post;
+			l->post = NULL;
+			orc_update(t->dilution, l->curr_subjs, t->variants, child.post, child.post, bbpa, (uint32_t)re, t->dil,
+					   t->orig_subjs + 1, 1);
+		}
+		if (!orc_update_with_shrinking(t, &child))
+		{
+			t->failed = 1;
+			return;
+		}
+		OrcNode *cn = &t->nodes[first + re];
+		cn->ex = ex;
+		cn->res = (uint32_t)re;
+		cn->stage = stage + 1;
+		cn->branch_prob = 0.0;
+		orc_build(t, first + re, &child);
+		if (t->failed)
+			return;
+	}
+}
+
+/* apply_true_state_helper, src/core/tree/tree.cpp:174-199. */
+static void orc_apply(const OrcTree *t, OrcNode *nodes, int node, uint32_t ts, double prob, double thres)
+{
+	nodes[node].branch_prob = prob;
+	if (nodes[node].first_child < 0)
+		return;
+	const int R = 1 << t->variants;
+	for (int i = 0; i < R; i++)
+	{
+		const int c = nodes[node].first_child + i;
+		const double child_prob = prob * orc_response_prob(t->dilution, t->orig_subjs, t->variants, nodes[c].ex,
+															nodes[c].res, ts, t->dil, t->orig_subjs + 1);
+		if (child_prob > thres)
+			orc_apply(t, nodes, c, ts, child_prob, thres);
+		else
+			nodes[c].branch_prob = 0.0;
+	}
+}
+
+typedef struct OrcStateStat
+{
+	double correct[31], incorrect[31], fp[31], fn[31];
+	double unclas, exp_stage, exp_test;
+} OrcStateStat;
+
+/* Tree::find_all_stat (tree.cpp:154-172) fused with the per-leaf body of
+ * Tree::parse (tree.cpp:70-111). */
+static void orc_parse_walk(const OrcTree *t, const OrcNode *nodes, int node, uint32_t ts, double coef, double thres,
+						   OrcStateStat *st)
+{
+	const OrcNode *nd = &nodes[node];
+	if (nd->branch_prob < thres)
+		return;
+	if (nd->first_child >= 0)
+	{
+		const int R = 1 << t->variants;
+		for (int i = 0; i < R; i++)
+			orc_parse_walk(t, nodes, nd->first_child + i, ts, coef, thres, st);
+		return;
+	}
+	const int index = nd->stage;
+	const double bp = nd->branch_prob;
+	const int classified = orc_is_classified(t, nd->pos, nd->neg);
+	if (classified && nd->neg == ts)
+	{
+		st->correct[index] += bp * coef;
+	}
+	else if (classified)
+	{
+		const double total_positive = (double)orc_popcount(nd->pos);
+		const double total_negative = (double)orc_popcount(nd->neg);
+		const double fp = total_positive == 0.0 ? 0.0 : orc_popcount((nd->neg ^ ts) & ts) / total_positive;
+		const double fn = total_negative == 0.0 ? 0.0 : orc_popcount((nd->neg ^ ts) & ~ts) / total_negative;
+		st->incorrect[index] += bp * coef;
+		st->fp[index] += fp * coef * bp;
+		st->fn[index] += fn * coef * bp;
+	}
+	else
+	{
+		st->unclas = st->unclas + bp;
+	}
+	st->exp_stage = st->exp_stage + ceil((double)index / (double)1) * bp;
+	st->exp_test = st->exp_test + index * bp;
+}
+
+/* bgt::run_simulation on the CPU provider for local_tree
+ * (src/runtime/simulation_runner.cpp:92-132 and :181-262): builds the tree
+ * from the prior, then sweeps every true state.  out[0] = total leaves,
+ * out[1..7] = correct, incorrect, false positive, false negative,
+ * unclassified, expected stages, expected tests.  Returns 0, 2 for an
+ * unsupported request (Op-BHA with k > 1), 4 on allocation failure. */
+ORC_EXPORT int orc_run_simulation(int dilution, int subjects, int variants, const double *pi0, int depth, double up,
+								  double lo, double branch, int selector, double alpha, double h, double *out)
+{
+	const int atoms = subjects * variants;
+	const int resolved = selector == 0 ? (variants == 1 ? 1 : 2) : selector;
+	if (resolved == 1 && variants != 1)
+		return 2;
+	OrcTree t;
+	memset(&t, 0, sizeof(t));
+	t.orig_subjs = subjects;
+	t.variants = variants;
+	t.depth = depth;
+	t.selector = resolved;
+	t.dilution = dilution;
+	t.up = up;
+	t.lo = lo;
+	double *dil = (double *)malloc(sizeof(double) * (size_t)subjects * (size_t)(subjects + 1));
+	t.scratch = (double *)malloc(sizeof(double) * ((size_t)1 << subjects) * (size_t)(1 << variants));
+	OrcLattice root;
+	memset(&root, 0, sizeof(root));
+	root.curr_subjs = subjects;
+	root.post = (double *)malloc(sizeof(double) * ((size_t)1 << atoms));
+	if (!dil || !t.scratch || !root.post)
+	{
+		free(dil);
+		free(t.scratch);
+		free(root.post);
+		return 4;
+	}
+	orc_dilution_table(subjects, alpha, h, dil);
+	t.dil = dil;
+	orc_prior(atoms, pi0, root.post);
+	const int r0 = orc_new_node(&t);
+	t.nodes[r0].ex = 0;
+	t.nodes[r0].res = 0;
+	t.nodes[r0].stage = 0;
+	t.nodes[r0].branch_prob = 0.0;
+	orc_build(&t, r0, &root);
+	free(root.post);
+	if (t.failed)
+	{
+		free(dil);
+		free(t.scratch);
+		free(t.nodes);
+		return 4;
+	}
+	int leaves = 0;
+	for (int i = 0; i < t.count; i++)
+		if (t.nodes[i].first_child < 0)
+			leaves++;
+	/* Leaves are counted by find_all_leaves (tree.cpp:134-152), which visits
+	 * every node; the node array holds each node exactly once. */
+	double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+	const size_t states = (size_t)1 << atoms;
+	for (size_t s = 0; s < states; s++)
+	{
+		const uint32_t ts = (uint32_t)s;
+		OrcStateStat st;
+		memset(&st, 0, sizeof(st));
+		orc_apply(&t, t.nodes, r0, ts, 1.0, branch);
+		const double coef = orc_prior_prob(atoms, pi0, ts) * 1.0;
+		orc_parse_walk(&t, t.nodes, r0, ts, coef, branch, &st);
+		st.unclas = st.unclas * coef;
+		st.exp_stage = st.exp_stage * coef;
+		st.exp_test = st.exp_test * coef;
+		/* accumulate_tree_stats, src/runtime/simulation_helpers.cpp:11-23. */
+		acc[4] += st.unclas;
+		acc[5] += st.exp_stage;
+		acc[6] += st.exp_test;
+		for (int i = 0; i <= depth * 1; i++)
+		{
+			acc[0] += st.correct[i];
+			acc[1] += st.incorrect[i];
+			acc[2] += st.fp[i];
+			acc[3] += st.fn[i];
+		}
+	}
+	out[0] = leaves;
+	for (int i = 0; i < 7; i++)
+		out[1 + i] = acc[i];
+	free(dil);
+	free(t.scratch);
+	free(t.nodes);
+	return 0;
+}

@@ -1,0 +1,307 @@
+"""ctypes access to the CPU parity oracles (test infrastructure only).
+
+Two oracles live here:
+
+* ``Oracle`` loads ``oracle/_build/libbgt_oracle.so``, the C restatement of
+  the reference's lattice hot path (``oracle/bgt_oracle.c``).  It builds with
+  plain ``gcc`` on any host, including the GPU machine.
+* ``Reference`` loads ``oracle/_ref/libbgtref*.so``: the reference library's
+  own CPU provider compiled unmodified from its sources by
+  ``oracle/ref/Makefile``.  It exists only where the reference sources are
+  present; the restatement is pinned against it there.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
+use this module, and only as the checker.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, c_double, c_int, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+BUILD_DIR = os.path.join(HERE, "_build")
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_SO = os.path.join(BUILD_DIR, "libbgt_oracle.so")
+
+NON_DILUTION, DILUTION = 0, 1
+AUTO, OP_BHA, OP_BBPA = 0, 1, 2
+
+_dp = POINTER(c_double)
+_up = POINTER(c_uint32)
+
+
+def _ptr(a: np.ndarray, kind=_dp):
+    return a.ctypes.data_as(kind)
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile the C restatement with IEEE semantics (no fast-math, no FMA
+    contraction, so x86 and Arm give the same bits)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    src = os.path.join(HERE, "bgt_oracle.c")
+    hdr = os.path.join(REPO, "include", "bgt_session_rng.h")
+    if (not force and os.path.exists(ORACLE_SO)
+            and os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return ORACLE_SO
+    tmp = ORACLE_SO + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-fvisibility=hidden", "-I", os.path.join(REPO, "include"), src, "-o", tmp, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_reference(ref_root: str = "/root/reference", jobs: int = 8) -> bool:
+    """Compile the reference CPU provider into oracle/_ref when its sources exist."""
+    if not os.path.isdir(os.path.join(ref_root, "src")):
+        return False
+    subprocess.run(["make", "-s", f"-j{jobs}", "-C", os.path.join(HERE, "ref"), f"REF_ROOT={ref_root}",
+                    f"OUT={REF_DIR}"], check=True)
+    return True
+
+
+def reference_available(strict: bool = True) -> bool:
+    return os.path.exists(os.path.join(REF_DIR, "libbgtref_strict.so" if strict else "libbgtref.so"))
+
+
+class Oracle:
+    """The C restatement (``orc_*`` entry points)."""
+
+    def __init__(self, path: str | None = None):
+        path = path or build_oracle()
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        L.orc_dilution_table.argtypes = [c_int, c_double, c_double, _dp]
+        L.orc_response_prob.argtypes = [c_int, c_int, c_int, c_uint32, c_uint32, c_uint32, _dp, c_int]
+        L.orc_response_prob.restype = c_double
+        L.orc_prior_prob.argtypes = [c_int, _dp, c_uint32]
+        L.orc_prior_prob.restype = c_double
+        L.orc_prior.argtypes = [c_int, _dp, _dp]
+        L.orc_update.argtypes = [c_int, c_int, c_int, _dp, _dp, c_uint32, c_uint32, _dp, c_int, c_int]
+        L.orc_update.restype = c_double
+        L.orc_atom_masses.argtypes = [_dp, c_int, _dp]
+        L.orc_classify.argtypes = [_dp, c_int, c_double, c_double, _up, _up]
+        L.orc_classify_masses.argtypes = [_dp, c_int, c_double, c_double, _up, _up]
+        L.orc_upset_mass.argtypes = [_dp, c_int, c_uint32]
+        L.orc_upset_mass.restype = c_double
+        L.orc_zeta.argtypes = [_dp, c_int]
+        L.orc_op_bha.argtypes = [_dp, c_int, _dp]
+        L.orc_op_bha.restype = c_uint32
+        L.orc_bbpa.argtypes = [_dp, c_int, c_int, c_double, _dp, _dp]
+        L.orc_bbpa.restype = c_uint32
+        L.orc_select.argtypes = [_dp, c_int, c_int, c_int, _dp]
+        L.orc_select.restype = c_uint32
+        L.orc_session.argtypes = [c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_double, c_int,
+                                  c_uint64, c_uint64, c_uint32, _up, _up, _up, _up, _dp]
+        L.orc_session.restype = c_int
+        L.orc_run_simulation.argtypes = [c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_int,
+                                         c_double, c_double, _dp]
+        L.orc_run_simulation.restype = c_int
+
+    # model -----------------------------------------------------------------
+    def dilution_table(self, n, alpha=0.99, h=0.005):
+        out = np.zeros(n * (n + 1))
+        self.lib.orc_dilution_table(n, alpha, h, _ptr(out))
+        return out.reshape(n, n + 1)
+
+    def prior(self, pi0, atoms=None):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        atoms = len(pi0) if atoms is None else atoms
+        out = np.empty(1 << atoms)
+        self.lib.orc_prior(atoms, _ptr(pi0), _ptr(out))
+        return out
+
+    def prior_prob(self, pi0, state):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        return self.lib.orc_prior_prob(len(pi0), _ptr(pi0), state)
+
+    def response_prob(self, dilution, n, k, e, r, s, alpha=0.99, h=0.005):
+        dil = self.dilution_table(n, alpha, h).ravel()
+        return self.lib.orc_response_prob(dilution, n, k, e, r, s, _ptr(dil), n + 1)
+
+    def update(self, dilution, n, k, post, e, r, alpha=0.99, h=0.005, in_place=True):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        out = np.empty_like(post)
+        dil = self.dilution_table(n, alpha, h).ravel()
+        self.lib.orc_update(dilution, n, k, _ptr(post), _ptr(out), e, r, _ptr(dil), n + 1, 1 if in_place else 0)
+        return out
+
+    def atom_masses(self, post, atoms):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        out = np.empty(atoms)
+        self.lib.orc_atom_masses(_ptr(post), atoms, _ptr(out))
+        return out
+
+    def classify(self, post, atoms, up, lo, pos=0, neg=0):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        p = np.array([pos], dtype=np.uint32)
+        q = np.array([neg], dtype=np.uint32)
+        self.lib.orc_classify(_ptr(post), atoms, up, lo, _ptr(p, _up), _ptr(q, _up))
+        return int(p[0]), int(q[0])
+
+    def upset_mass(self, post, atoms, e):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        return self.lib.orc_upset_mass(_ptr(post), atoms, e)
+
+    # selectors -------------------------------------------------------------
+    def zeta(self, a, bits):
+        a = np.array(a, dtype=np.float64, copy=True)
+        self.lib.orc_zeta(_ptr(a), bits)
+        return a
+
+    def op_bha(self, post, n):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        scratch = np.empty(1 << n)
+        e = self.lib.orc_op_bha(_ptr(post), n, _ptr(scratch))
+        return int(e), scratch
+
+    def bbpa(self, post, n, k, target=None):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        target = 1.0 / (1 << k) if target is None else target
+        table = np.empty((1 << n) * (1 << k))
+        best = np.zeros(1)
+        e = self.lib.orc_bbpa(_ptr(post), n, k, target, _ptr(table), _ptr(best))
+        return int(e), float(best[0]), table
+
+    def select(self, post, n, k, selector=AUTO):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        scratch = np.empty((1 << n) * (1 << k))
+        return int(self.lib.orc_select(_ptr(post), n, k, selector, _ptr(scratch)))
+
+    # drivers ---------------------------------------------------------------
+    def session(self, dilution, n, k, pi0, stages, seed, session, true_state, selector=AUTO, alpha=0.99,
+                h=0.005, up=0.01, lo=0.01):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        ex = np.zeros(stages, np.uint32)
+        rs = np.zeros(stages, np.uint32)
+        pm = np.zeros(stages, np.uint32)
+        nm = np.zeros(stages, np.uint32)
+        post = np.empty(1 << (n * k))
+        rc = self.lib.orc_session(dilution, n, k, _ptr(pi0), selector, alpha, h, up, lo, stages, seed, session,
+                                  true_state, _ptr(ex, _up), _ptr(rs, _up), _ptr(pm, _up), _ptr(nm, _up),
+                                  _ptr(post))
+        if rc != 0:
+            raise RuntimeError(f"oracle session failed ({rc})")
+        return dict(experiments=ex, responses=rs, pos=pm, neg=nm, posterior=post)
+
+    def run_simulation(self, dilution, n, k, pi0, depth, up=0.01, lo=0.01, branch=0.0, selector=AUTO,
+                       alpha=0.99, h=0.005):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        out = np.zeros(8)
+        rc = self.lib.orc_run_simulation(dilution, n, k, _ptr(pi0), depth, up, lo, branch, selector, alpha, h,
+                                         _ptr(out))
+        if rc != 0:
+            raise RuntimeError(f"oracle run_simulation failed ({rc})")
+        return out
+
+
+class Reference:
+    """The reference CPU provider itself (``ref_*`` entry points of oracle/ref/ref_shim.cpp)."""
+
+    def __init__(self, strict: bool = True):
+        name = "libbgtref_strict.so" if strict else "libbgtref.so"
+        self.lib = ctypes.CDLL(os.path.join(REF_DIR, name))
+        L = self.lib
+        L.ref_last_error.restype = ctypes.c_char_p
+        L.ref_prior.argtypes = [c_int, c_int, c_int, _dp, _dp]
+        L.ref_dilution_table.argtypes = [c_int, c_double, c_double, _dp]
+        L.ref_response_prob.argtypes = [c_int, c_int, c_int, _dp, c_uint32, c_uint32, c_uint32, c_double,
+                                        c_double, _dp]
+        L.ref_update.argtypes = [c_int, c_int, c_int, _dp, _dp, c_uint32, c_uint32, c_double, c_double, c_int, _dp]
+        L.ref_atom_masses.argtypes = [c_int, c_int, c_int, _dp, _dp, _dp]
+        L.ref_upset_mass.argtypes = [c_int, c_int, c_int, _dp, _dp, c_uint32, _dp]
+        L.ref_select.argtypes = [c_int, c_int, c_int, _dp, _dp, c_int, _up]
+        L.ref_classify.argtypes = [c_int, c_int, c_int, _dp, _dp, c_double, c_double, _up, _up]
+        L.ref_run_simulation.argtypes = [c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_int,
+                                         c_double, c_double, _dp]
+        L.ref_session.argtypes = [c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_double, c_int,
+                                  c_uint64, c_uint64, c_uint32, _up, _up, _up, _up, _dp]
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(self.lib.ref_last_error().decode())
+
+    @staticmethod
+    def _type(dilution):
+        return 4 if dilution else 3
+
+    def prior(self, pi0, k=1):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        n = len(pi0) // k
+        out = np.empty(1 << len(pi0))
+        self._check(self.lib.ref_prior(3, n, k, _ptr(pi0), _ptr(out)))
+        return out
+
+    def dilution_table(self, n, alpha=0.99, h=0.005):
+        out = np.zeros(n * (n + 1))
+        self._check(self.lib.ref_dilution_table(n, alpha, h, _ptr(out)))
+        return out.reshape(n, n + 1)
+
+    def response_prob(self, dilution, n, k, e, r, s, alpha=0.99, h=0.005):
+        pi0 = np.full(n * k, 0.1)
+        out = np.zeros(1)
+        self._check(self.lib.ref_response_prob(self._type(dilution), n, k, _ptr(pi0), e, r, s, alpha, h, _ptr(out)))
+        return float(out[0])
+
+    def update(self, dilution, n, k, post, e, r, alpha=0.99, h=0.005, in_place=True):
+        pi0 = np.full(n * k, 0.1)
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        out = np.empty_like(post)
+        self._check(self.lib.ref_update(self._type(dilution), n, k, _ptr(pi0), _ptr(post), e, r, alpha, h,
+                                        1 if in_place else 0, _ptr(out)))
+        return out
+
+    def atom_masses(self, post, n, k=1):
+        pi0 = np.full(n * k, 0.1)
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        out = np.empty(n * k)
+        self._check(self.lib.ref_atom_masses(3, n, k, _ptr(pi0), _ptr(post), _ptr(out)))
+        return out
+
+    def upset_mass(self, post, n, k, e):
+        pi0 = np.full(n * k, 0.1)
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        out = np.zeros(1)
+        self._check(self.lib.ref_upset_mass(3, n, k, _ptr(pi0), _ptr(post), e, _ptr(out)))
+        return float(out[0])
+
+    def select(self, post, n, k, selector=AUTO):
+        pi0 = np.full(n * k, 0.1)
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        out = np.zeros(1, np.uint32)
+        self._check(self.lib.ref_select(3, n, k, _ptr(pi0), _ptr(post), selector, _ptr(out, _up)))
+        return int(out[0])
+
+    def classify(self, post, n, k, up, lo, pos=0, neg=0):
+        pi0 = np.full(n * k, 0.1)
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        p = np.array([pos], np.uint32)
+        q = np.array([neg], np.uint32)
+        self._check(self.lib.ref_classify(3, n, k, _ptr(pi0), _ptr(post), up, lo, _ptr(p, _up), _ptr(q, _up)))
+        return int(p[0]), int(q[0])
+
+    def run_simulation(self, dilution, n, k, pi0, depth, up=0.01, lo=0.01, branch=0.0, selector=AUTO,
+                       alpha=0.99, h=0.005):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        out = np.zeros(8)
+        self._check(self.lib.ref_run_simulation(self._type(dilution), n, k, _ptr(pi0), depth, up, lo, branch,
+                                                selector, alpha, h, _ptr(out)))
+        return out
+
+    def session(self, dilution, n, k, pi0, stages, seed, session, true_state, selector=AUTO, alpha=0.99,
+                h=0.005, up=0.01, lo=0.01):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        ex = np.zeros(stages, np.uint32)
+        rs = np.zeros(stages, np.uint32)
+        pm = np.zeros(stages, np.uint32)
+        nm = np.zeros(stages, np.uint32)
+        post = np.empty(1 << (n * k))
+        self._check(self.lib.ref_session(self._type(dilution), n, k, _ptr(pi0), selector, alpha, h, up, lo, stages,
+                                         seed, session, true_state, _ptr(ex, _up), _ptr(rs, _up), _ptr(pm, _up),
+                                         _ptr(nm, _up), _ptr(post)))
+        return dict(experiments=ex, responses=rs, pos=pm, neg=nm, posterior=post)

@@ -1,0 +1,53 @@
+// Build configuration for compiling the reference CPU provider as the parity
+// oracle (test infrastructure only).  It supplies the values the reference's
+// CMake configure step would write: 32-bit state words, FP64 posterior and
+// accumulator, SIMD on, OpenMP/CUDA/NCCL off.  BGT_ORACLE_POSTERIOR_BITS can be
+// overridden on the command line to build an FP32-posterior oracle.
+#pragma once
+
+#ifndef BGT_ORACLE_POSTERIOR_BITS
+#define BGT_ORACLE_POSTERIOR_BITS 64
+#endif
+
+#define BGT_MAJOR 1
+#define BGT_MINOR 0
+#define BGT_PATCH 0
+#define BGT_SUFFIX ""
+#define BGT_VERSION_CODE 100
+#define BGT_ENABLE_SIMD 1
+#define BGT_ENABLE_FAST_MATH 1
+#define BGT_STATE_BITS 32
+#define BGT_POSTERIOR_BITS BGT_ORACLE_POSTERIOR_BITS
+#if BGT_ORACLE_POSTERIOR_BITS == 32
+#define BGT_POSTERIOR_PRECISION "float32"
+#else
+#define BGT_POSTERIOR_PRECISION "float64"
+#endif
+#define BGT_ACCUMULATOR_BITS 64
+#define BGT_ACCUMULATOR_PRECISION "float64"
+#define BGT_OPTIMIZATION_LEVEL_CODE 1
+#define BGT_PROFILE_BACKEND_CODE 0
+
+namespace bgt
+{
+inline constexpr int version_major = BGT_MAJOR;
+inline constexpr int version_minor = BGT_MINOR;
+inline constexpr int version_patch = BGT_PATCH;
+inline constexpr const char *version_suffix = BGT_SUFFIX;
+inline constexpr int version_code = BGT_VERSION_CODE;
+inline constexpr int state_bits = BGT_STATE_BITS;
+inline constexpr int posterior_bits = BGT_POSTERIOR_BITS;
+inline constexpr const char *posterior_precision_name = BGT_POSTERIOR_PRECISION;
+inline constexpr int accumulator_bits = BGT_ACCUMULATOR_BITS;
+inline constexpr const char *accumulator_precision_name = BGT_ACCUMULATOR_PRECISION;
+inline constexpr int optimization_level_code = BGT_OPTIMIZATION_LEVEL_CODE;
+inline constexpr int profile_backend_code = BGT_PROFILE_BACKEND_CODE;
+inline constexpr bool cuda_compiled = false;
+inline constexpr bool nccl_compiled = false;
+inline constexpr bool nccl_gin_compiled = false;
+inline constexpr bool simd_compiled = true;
+inline constexpr bool openmp_compiled = false;
+inline constexpr bool native_cpu_compiled = true;
+inline constexpr bool fast_math_compiled = true;
+inline constexpr bool caliper_profiling_compiled = false;
+} // namespace bgt
