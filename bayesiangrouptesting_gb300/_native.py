@@ -1,0 +1,95 @@
+"""ctypes binding of libbgt_gb300.so (the C ABI declared in include/bgt_gpu.h).
+
+The library is loaded from the package's in-tree build directory.  There is
+no fallback: if the library is missing or no GPU is present, the calls fail
+with an error instead of computing anything on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_uint32, c_uint64, c_void_p
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libbgt_gb300.so")
+
+_dp = POINTER(c_double)
+_up = POINTER(c_uint32)
+
+
+class TreeStatsC(ctypes.Structure):
+    """Layout of bgt_tree_stats / bgt::TreeStats (include/bgt/types.hpp:109-119)."""
+
+    _fields_ = [
+        ("total_leaves", c_int),
+        ("correct_probability", c_double),
+        ("incorrect_probability", c_double),
+        ("false_positive_probability", c_double),
+        ("false_negative_probability", c_double),
+        ("unclassified_probability", c_double),
+        ("expected_stages", c_double),
+        ("expected_tests", c_double),
+    ]
+
+
+# Every symbol the header declares, with its ctypes signature.
+SIGNATURES = {
+    "bgt_cuda_provider_available": ([], c_int),
+    "bgt_cuda_provider_run": ([c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_int,
+                               POINTER(_dp), POINTER(TreeStatsC)], c_int),
+    "bgt_cuda_provider_benchmark_select": ([c_int, c_int, _dp, c_int, c_int, c_int, _up, _dp, _dp, _dp, _dp, _dp],
+                                           c_int),
+    "bgt_gpu_lattice_create": ([c_int, c_int, c_int, _dp, c_int, POINTER(c_void_p)], c_int),
+    "bgt_gpu_lattice_destroy": ([c_void_p], c_int),
+    "bgt_gpu_lattice_set_stream": ([c_void_p, c_void_p], c_int),
+    "bgt_gpu_lattice_select": ([c_void_p, c_int, _up], c_int),
+    "bgt_gpu_lattice_reselect": ([c_void_p, c_int, _up], c_int),
+    "bgt_gpu_lattice_update": ([c_void_p, c_uint32, c_uint32, POINTER(_dp)], c_int),
+    "bgt_gpu_lattice_classify": ([c_void_p, c_double, c_double, _up, _up], c_int),
+    "bgt_gpu_lattice_read_posterior": ([c_void_p, _dp], c_int),
+    "bgt_gpu_lattice_posterior_probability": ([c_void_p, c_uint32, _dp], c_int),
+    "bgt_gpu_lattice_upset_mass": ([c_void_p, c_uint32, _dp], c_int),
+    "bgt_gpu_lattice_atom_masses": ([c_void_p, _dp], c_int),
+    "bgt_gpu_session_run": ([c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_uint64, c_uint64,
+                             c_uint32, _up, _up, _up, _up], c_int),
+    "bgt_gpu_last_error": ([], c_char_p),
+    "bgt_gpu_kernel_launch_count": ([], c_uint64),
+}
+
+_lib = None
+
+
+class NativeError(RuntimeError):
+    """A C-ABI call returned a non-zero status (reference codes 1, 2, 4)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"status {status}: {message}")
+        self.status = status
+
+
+def load(path: str | None = None):
+    """Load (once) and return the CDLL with every signature bound."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA provider library not built: {path} (run __graft_entry__.build())")
+    lib = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path == LIB_PATH:
+        _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        msg = load().bgt_gpu_last_error()
+        raise NativeError(status, msg.decode() if msg else "")
+
+
+def launches() -> int:
+    return int(load().bgt_gpu_kernel_launch_count())

@@ -1,0 +1,394 @@
+"""Python mirror of the reference's public lattice / runtime API for the hot path.
+
+Names, argument meanings and error behaviour follow the reference's
+nanobind module (src/bindings/python/bgt_module.cpp) and C++ headers
+(include/bgt/lattice.hpp, include/bgt/runtime.hpp, include/bgt/types.hpp,
+include/bgt/simulation.hpp), restricted to what the GPU provider serves:
+``Lattice`` sessions and ``run_simulation`` on ``Provider.cuda``.  Every call
+goes through the C ABI of include/bgt_gpu.h; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _native
+from ._native import NativeError, TreeStatsC, check, load
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_up = ctypes.POINTER(ctypes.c_uint32)
+
+
+class LatticeType(enum.IntEnum):
+    """bgt::LatticeType (include/bgt/types.hpp:81-87)."""
+
+    distributed_non_dilution = 0
+    distributed_dilution = 1
+    replicated_non_dilution = 2
+    replicated_dilution = 3
+
+
+class SelectorType(enum.IntEnum):
+    """bgt::SelectorType (include/bgt/types.hpp:89-94)."""
+
+    auto_select = 0
+    op_bha = 1
+    op_bbpa = 2
+
+
+class Provider(enum.IntEnum):
+    """bgt::Provider (include/bgt/types.hpp:96-101)."""
+
+    auto_select = 0
+    cpu = 1
+    cuda = 2
+
+
+class Precision(enum.IntEnum):
+    """bgt::Precision (include/bgt/compile_options.hpp:20-24) mapped to the
+    device lattice's storage precision."""
+
+    float32 = 0
+    float64 = 1
+
+
+class StatusCode(enum.IntEnum):
+    """bgt::StatusCode (include/bgt/status.hpp:10-19)."""
+
+    success = 0
+    invalid_argument = 1
+    unsupported = 2
+    runtime_error = 3
+    mpi_error = 4
+    cuda_error = 5
+    internal_error = 6
+
+
+class Error(RuntimeError):
+    """bgt::Error (include/bgt/status.hpp:42-50): carries a StatusCode."""
+
+    def __init__(self, code: StatusCode, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+def _raise_from(exc: NativeError):
+    if exc.status == 1:
+        raise ValueError(str(exc)) from None
+    if exc.status == 2:
+        raise Error(StatusCode.unsupported, str(exc)) from None
+    raise Error(StatusCode.cuda_error, str(exc)) from None
+
+
+def _call(status: int) -> None:
+    try:
+        check(status)
+    except NativeError as exc:
+        _raise_from(exc)
+
+
+def _uses_dilution(t: LatticeType) -> bool:
+    return t in (LatticeType.replicated_dilution, LatticeType.distributed_dilution)
+
+
+def _resolve_selector(selector: SelectorType, variants: int) -> SelectorType:
+    """resolve_selector, src/runtime/simulation_helpers.cpp:40-45."""
+    if selector == SelectorType.auto_select:
+        return SelectorType.op_bha if variants == 1 else SelectorType.op_bbpa
+    return SelectorType(selector)
+
+
+def reverse_bits(value: int, width: int) -> int:
+    """Public <-> internal subject order for binary lattices
+    (reverse_bits, src/core/lattice_api.cpp:17-26)."""
+    ret = 0
+    for i in range(width):
+        ret = (ret << 1) | ((value >> i) & 1)
+    return ret
+
+
+class DilutionTable:
+    """bgt::DilutionTable (include/bgt/lattice.hpp:17-32; src/core/model/dilution.cpp:44-71)."""
+
+    def __init__(self, subjects: int, alpha: float, h: float):
+        if subjects <= 0:
+            raise ValueError("subjects must be positive.")
+        self._subjects = subjects
+        self.alpha = float(alpha)
+        self.h = float(h)
+        n = subjects
+        values = np.zeros((n, n + 1), dtype=np.float64)
+        for rk in range(1, n + 1):
+            values[rk - 1, 0] = alpha
+            for r in range(1, rk + 1):
+                k = rk - r
+                values[rk - 1, r] = 1 - alpha * r / (k * h + r)
+        self._values = values
+        self._rows = (_dp * n)(*[values[i].ctypes.data_as(_dp) for i in range(n)])
+
+    @property
+    def subjects(self) -> int:
+        return self._subjects
+
+    def at(self, group_size: int, positives: int) -> float:
+        if group_size <= 0 or group_size > self._subjects or positives < 0 or positives > group_size:
+            raise IndexError("dilution table index is out of range.")
+        return float(self._values[group_size - 1, positives])
+
+    def rows(self):
+        return self._rows
+
+    def as_array(self) -> np.ndarray:
+        return self._values
+
+
+@dataclass
+class TreeStats:
+    """bgt::TreeStats (include/bgt/types.hpp:109-119)."""
+
+    total_leaves: int = 0
+    correct_probability: float = 0.0
+    incorrect_probability: float = 0.0
+    false_positive_probability: float = 0.0
+    false_negative_probability: float = 0.0
+    unclassified_probability: float = 0.0
+    expected_stages: float = 0.0
+    expected_tests: float = 0.0
+
+    @classmethod
+    def from_c(cls, c: TreeStatsC) -> "TreeStats":
+        return cls(c.total_leaves, c.correct_probability, c.incorrect_probability, c.false_positive_probability,
+                   c.false_negative_probability, c.unclassified_probability, c.expected_stages, c.expected_tests)
+
+    def as_array(self) -> np.ndarray:
+        return np.array([self.total_leaves, self.correct_probability, self.incorrect_probability,
+                         self.false_positive_probability, self.false_negative_probability,
+                         self.unclassified_probability, self.expected_stages, self.expected_tests])
+
+
+@dataclass
+class SimulationOptions:
+    """bgt::SimulationOptions (include/bgt/types.hpp:121-130)."""
+
+    search_depth: int = 1
+    threshold_up: float = 0.01
+    threshold_lo: float = 0.01
+    branch_threshold: float = 0.0
+    selector: SelectorType = SelectorType.auto_select
+    provider: Provider = Provider.auto_select
+
+
+@dataclass
+class DilutionParameters:
+    """bgt::DilutionParameters (include/bgt/simulation.hpp:44-48)."""
+
+    alpha: float = 0.99
+    h: float = 0.005
+
+
+@dataclass
+class SimulationConfig:
+    """The local_tree subset of bgt::SimulationConfig (include/bgt/simulation.hpp:87-103)."""
+
+    lattice_type: LatticeType = LatticeType.replicated_non_dilution
+    subjects: int = 0
+    variants: int = 1
+    prior: Sequence[float] = field(default_factory=list)
+    options: SimulationOptions = field(default_factory=SimulationOptions)
+    dilution: DilutionParameters = field(default_factory=DilutionParameters)
+
+
+@dataclass
+class SimulationResult:
+    """The local_tree subset of bgt::SimulationResult (include/bgt/simulation.hpp:105-121)."""
+
+    stats: TreeStats
+    provider: Provider
+    total_states: int
+    evaluated_states: int
+
+
+def cuda_available() -> bool:
+    """bgt::cuda_available (src/runtime/providers.cpp:136-139)."""
+    try:
+        return bool(load().bgt_cuda_provider_available())
+    except RuntimeError:
+        return False
+
+
+def available_providers():
+    return [Provider.cpu] + ([Provider.cuda] if cuda_available() else [])
+
+
+def _validate(config: SimulationConfig) -> None:
+    """validate_simulation_config, src/runtime/simulation_runner.cpp:30-68 (local_tree part)."""
+    o = config.options
+    if config.subjects <= 0 or config.variants <= 0 or o.search_depth < 0:
+        raise ValueError("invalid simulation dimensions.")
+    if len(config.prior) != config.subjects * config.variants:
+        raise ValueError("prior length must equal subjects * variants.")
+    if _resolve_selector(o.selector, config.variants) == SelectorType.op_bha and config.variants != 1:
+        raise ValueError("Op-BHA tree selection is only supported for binary lattices.")
+    if _uses_dilution(config.lattice_type) and (config.dilution.alpha <= 0.0 or config.dilution.h <= 0.0):
+        raise ValueError("dilution parameters must be positive.")
+    if config.lattice_type in (LatticeType.distributed_non_dilution, LatticeType.distributed_dilution):
+        raise ValueError("local_tree requires a replicated lattice.")
+
+
+def run_simulation(config: SimulationConfig) -> SimulationResult:
+    """bgt::run_simulation for local_tree on the GPU provider
+    (Runtime::run_simulation, src/runtime/simulation_runner.cpp:181-262, via
+    CudaProvider::run, src/runtime/providers.cpp:73-133).  Provider.cpu is the
+    reference library's own provider and is not served here; Provider.cuda
+    and auto_select run on the device or raise."""
+    _validate(config)
+    if config.options.provider == Provider.cpu:
+        raise Error(StatusCode.unsupported, "the CPU provider is the reference library's; this package is the CUDA provider")
+    lib = load()
+    if not lib.bgt_cuda_provider_available():
+        raise Error(StatusCode.cuda_error, "CUDA provider requested, but no CUDA device is available.")
+    prior = np.ascontiguousarray(config.prior, dtype=np.float64)
+    dil = None
+    if _uses_dilution(config.lattice_type):
+        dil = DilutionTable(config.subjects, config.dilution.alpha, config.dilution.h)
+    stats = TreeStatsC()
+    status = lib.bgt_cuda_provider_run(1 if dil else 0, config.subjects, config.variants, prior.ctypes.data_as(_dp),
+                                       config.options.search_depth, config.options.threshold_up,
+                                       config.options.threshold_lo, config.options.branch_threshold,
+                                       int(_resolve_selector(config.options.selector, config.variants)),
+                                       dil.rows() if dil else None, ctypes.byref(stats))
+    _call(status)
+    total = 1 << (config.subjects * config.variants)
+    return SimulationResult(TreeStats.from_c(stats), Provider.cuda, total, total)
+
+
+class Lattice:
+    """GPU-backed bgt::Lattice (include/bgt/lattice.hpp:34-67; CPU counterpart
+    src/core/lattice_api.cpp:61-196).  For binary lattices the public subject
+    order is bit-reversed relative to the internal order, as in the reference."""
+
+    def __init__(self, type: LatticeType, subjects: int, prior, variants: int = 1,
+                 precision: Precision = Precision.float64):
+        if subjects <= 0 or variants <= 0:
+            raise ValueError("subjects and variants must be positive.")
+        prior = np.ascontiguousarray(prior, dtype=np.float64)
+        if prior.size != subjects * variants:
+            raise ValueError("prior length must equal subjects * variants.")
+        self._type = LatticeType(type)
+        self._subjects = subjects
+        self._variants = variants
+        self._prior = prior
+        self._handle = ctypes.c_void_p()
+        self._lib = load()
+        status = self._lib.bgt_gpu_lattice_create(1 if _uses_dilution(self._type) else 0, subjects, variants,
+                                                  prior.ctypes.data_as(_dp),
+                                                  0 if precision == Precision.float64 else 1,
+                                                  ctypes.byref(self._handle))
+        _call(status)
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            self._lib.bgt_gpu_lattice_destroy(h)
+            self._handle = None
+
+    # -- shape ---------------------------------------------------------------
+    @property
+    def subjects(self) -> int:
+        return self._subjects
+
+    @property
+    def variants(self) -> int:
+        return self._variants
+
+    @property
+    def type(self) -> LatticeType:
+        return self._type
+
+    @property
+    def handle(self):
+        return self._handle
+
+    def _to_internal(self, value: int) -> int:
+        return reverse_bits(value, self._subjects) if self._variants == 1 else value
+
+    _to_public = _to_internal
+
+    # -- queries -------------------------------------------------------------
+    def posterior_probability(self, state: int) -> float:
+        out = ctypes.c_double()
+        _call(self._lib.bgt_gpu_lattice_posterior_probability(self._handle, self._to_internal(state),
+                                                              ctypes.byref(out)))
+        return out.value
+
+    def upset_probability_mass(self, experiment: int) -> float:
+        out = ctypes.c_double()
+        _call(self._lib.bgt_gpu_lattice_upset_mass(self._handle, self._to_internal(experiment), ctypes.byref(out)))
+        return out.value
+
+    def posterior(self) -> np.ndarray:
+        """The whole normalised posterior in internal state order."""
+        out = np.empty(1 << (self._subjects * self._variants))
+        _call(self._lib.bgt_gpu_lattice_read_posterior(self._handle, out.ctypes.data_as(_dp)))
+        return out
+
+    def atom_masses(self) -> np.ndarray:
+        out = np.empty(self._subjects * self._variants)
+        _call(self._lib.bgt_gpu_lattice_atom_masses(self._handle, out.ctypes.data_as(_dp)))
+        return out
+
+    # -- session -------------------------------------------------------------
+    def select_experiment(self, selector: SelectorType = SelectorType.auto_select) -> int:
+        out = ctypes.c_uint32()
+        _call(self._lib.bgt_gpu_lattice_select(self._handle, int(selector), ctypes.byref(out)))
+        return self._to_public(out.value)
+
+    def update(self, experiment: int, response: int, dilution: Optional[DilutionTable] = None) -> None:
+        if _uses_dilution(self._type) and dilution is None:
+            raise ValueError("dilution table is required for dilution models.")
+        rows = dilution.rows() if dilution is not None else None
+        _call(self._lib.bgt_gpu_lattice_update(self._handle, self._to_internal(experiment), response, rows))
+
+    def update_classification(self, threshold_up: float, threshold_lo: float) -> None:
+        p = ctypes.c_uint32()
+        n = ctypes.c_uint32()
+        _call(self._lib.bgt_gpu_lattice_classify(self._handle, threshold_up, threshold_lo, ctypes.byref(p),
+                                                 ctypes.byref(n)))
+        self._pos, self._neg = p.value, n.value
+
+    def positive_classification_mask(self) -> int:
+        return self._to_public(getattr(self, "_pos", 0))
+
+    def negative_classification_mask(self) -> int:
+        return self._to_public(getattr(self, "_neg", 0))
+
+    def is_classified(self) -> bool:
+        atoms = self._subjects * self._variants
+        return bin(getattr(self, "_pos", 0) | getattr(self, "_neg", 0)).count("1") == atoms
+
+    def run_session(self, stages: int, true_state: int, seed: int, session: int = 0,
+                    selector: SelectorType = SelectorType.auto_select, alpha: float = 0.99, h: float = 0.005,
+                    threshold_up: float = 0.01, threshold_lo: float = 0.01):
+        """Device-driven adaptive session (bgt_gpu_session_run); internal bit order."""
+        ex = np.zeros(stages, np.uint32)
+        rs = np.zeros(stages, np.uint32)
+        pm = np.zeros(stages, np.uint32)
+        nm = np.zeros(stages, np.uint32)
+        _call(self._lib.bgt_gpu_session_run(self._handle, int(selector), stages, alpha, h, threshold_up, threshold_lo,
+                                            seed, session, true_state, ex.ctypes.data_as(_up), rs.ctypes.data_as(_up),
+                                            pm.ctypes.data_as(_up), nm.ctypes.data_as(_up)))
+        if stages:
+            self._pos, self._neg = int(pm[-1]), int(nm[-1])
+        return dict(experiments=ex, responses=rs, pos=pm, neg=nm)
+
+
+def select_experiment(lattice: Lattice, selector: SelectorType = SelectorType.auto_select) -> int:
+    return lattice.select_experiment(selector)
+
+
+def update(lattice: Lattice, experiment: int, response: int, dilution: Optional[DilutionTable] = None) -> None:
+    lattice.update(experiment, response, dilution)

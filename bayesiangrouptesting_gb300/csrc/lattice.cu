@@ -1,0 +1,705 @@
+// Host side of the GB300 lattice provider: device-lattice handles, stage
+// orchestration (K1 / K2, see lattice_kernels.cuh) and the C ABI of
+// include/bgt_gpu.h.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bgt_gpu.h"
+#include "lattice_kernels.cuh"
+#include "provider_internal.h"
+
+namespace bgt_gpu
+{
+
+__global__ void k1_zeta_low(LatticeDev *states);
+__global__ void k2_zeta_high_select(LatticeDev *states);
+__global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
+__global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, unsigned long long *out);
+
+namespace
+{
+thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
+} // namespace
+
+void set_error(const std::string &message) { g_last_error = message; }
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+void cuda_check(cudaError_t err, const char *what)
+{
+	if (err != cudaSuccess)
+		throw CudaFailure(std::string(what) + ": " + cudaGetErrorString(err));
+}
+
+size_t k1_smem_bytes() { return sizeof(unsigned long long) << kTileBits; }
+size_t k2_smem_bytes(int hbits) { return (sizeof(unsigned long long) * kColW + sizeof(int)) << hbits; }
+
+void configure_kernels()
+{
+	static bool done = false;
+	if (done)
+		return;
+	cuda_check(cudaFuncSetAttribute(k1_zeta_low, cudaFuncAttributeMaxDynamicSharedMemorySize,
+									static_cast<int>(k1_smem_bytes())),
+			   "k1 smem attribute");
+	cuda_check(cudaFuncSetAttribute(k2_zeta_high_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
+									static_cast<int>(k2_smem_bytes(kMaxHighBits))),
+			   "k2 smem attribute");
+	done = true;
+}
+
+void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream)
+{
+	dim3 grid(1u << g.hbits, static_cast<unsigned>(count));
+	k1_zeta_low<<<grid, kTileThreads, k1_smem_bytes(), stream>>>(states);
+	cuda_check(cudaGetLastError(), "k1 launch");
+	count_launches(1);
+}
+
+void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream)
+{
+	dim3 grid(static_cast<unsigned>(g.nblk), static_cast<unsigned>(count));
+	k2_zeta_high_select<<<grid, kHighThreads, k2_smem_bytes(g.hbits), stream>>>(states);
+	cuda_check(cudaGetLastError(), "k2 launch");
+	count_launches(1);
+}
+
+LatticeGeometry make_geometry(int n, int k)
+{
+	LatticeGeometry g;
+	g.n = n;
+	g.k = k;
+	g.atoms = n * k;
+	g.tbits = g.atoms < kTileBits ? g.atoms : kTileBits;
+	g.hbits = g.atoms - g.tbits;
+	g.nblk = (1 << g.tbits) >= kColW ? (1 << g.tbits) / kColW : 1;
+	return g;
+}
+
+// Validates a request against what this build supports; returns 0 or a status.
+int check_supported(int subjects, int variants, std::string *why)
+{
+	if (subjects <= 0 || variants <= 0)
+	{
+		*why = "subjects and variants must be positive";
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (subjects * variants > kMaxAtoms)
+	{
+		*why = "subjects * variants exceeds 30 atoms";
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (variants != 1)
+	{
+		*why = "multinomial (variants > 1) lattices are not supported by this build";
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (subjects > kTileBits + kMaxHighBits)
+	{
+		*why = "binary lattices above 24 subjects are not supported by this build";
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return 0;
+}
+
+std::vector<double> flatten_dilution(const double *const *rows, int n)
+{
+	std::vector<double> flat(static_cast<size_t>(n) * (n + 1), 0.0);
+	for (int L = 1; L <= n; L++)
+		for (int c = 0; c <= L; c++)
+			flat[static_cast<size_t>(L - 1) * (n + 1) + c] = rows[L - 1][c];
+	return flat;
+}
+
+} // namespace bgt_gpu
+
+using namespace bgt_gpu;
+
+// ---------------------------------------------------------------- lattice
+
+struct bgt_gpu_lattice
+{
+	LatticeGeometry g;
+	int dilution = 0;
+	int precision = 0;
+	cudaStream_t own_stream = nullptr;
+	cudaStream_t stream = nullptr;
+	LatticeDev host{};          // host mirror of the host-set fields
+	LatticeDev *dev = nullptr;  // device state
+	double *q = nullptr;
+	unsigned long long *m1 = nullptr;
+	unsigned long long *tile_total = nullptr;
+	int *tile_scale = nullptr;
+	unsigned long long *blk_score = nullptr;
+	unsigned int *blk_e = nullptr;
+	double *dil = nullptr;
+	double *prior_lo = nullptr, *prior_hi = nullptr, *pi0 = nullptr;
+	unsigned long long *scratch_u64 = nullptr;
+	unsigned int *sess_out = nullptr; // 4 * max stages
+	int sess_capacity = 0;
+	bool have_dilution = false;
+	// Host-side view of the device pipeline.
+	bool k1_pending = true;   // a K1 must run before the zeta partial sums are current
+	bool k2_valid = false;    // K2 results (selection, atom masses) are current
+	bool update_pending = false;
+	uint32_t pos = 0, neg = 0;
+
+	~bgt_gpu_lattice()
+	{
+		cudaFree(dev);
+		cudaFree(q);
+		cudaFree(m1);
+		cudaFree(tile_total);
+		cudaFree(tile_scale);
+		cudaFree(blk_score);
+		cudaFree(blk_e);
+		cudaFree(dil);
+		cudaFree(prior_lo);
+		cudaFree(prior_hi);
+		cudaFree(pi0);
+		cudaFree(scratch_u64);
+		cudaFree(sess_out);
+		if (own_stream)
+			cudaStreamDestroy(own_stream);
+	}
+
+	template <typename T>
+	void set_field(size_t offset, const T &value)
+	{
+		cuda_check(cudaMemcpyAsync(reinterpret_cast<char *>(dev) + offset, &value, sizeof(T), cudaMemcpyHostToDevice,
+								   stream),
+				   "state write");
+	}
+
+	template <typename T>
+	T get_field(size_t offset)
+	{
+		T value{};
+		cuda_check(cudaMemcpyAsync(&value, reinterpret_cast<char *>(dev) + offset, sizeof(T), cudaMemcpyDeviceToHost,
+								   stream),
+				   "state read");
+		cuda_check(cudaStreamSynchronize(stream), "state read sync");
+		return value;
+	}
+
+	void check_device_error()
+	{
+		const int err = get_field<int>(offsetof(LatticeDev, error));
+		if (err == kErrZeroMass)
+			throw CudaFailure("posterior normalising constant is zero");
+		if (err == kErrNonFinite)
+			throw CudaFailure("non-finite posterior value");
+	}
+
+	void run_k1()
+	{
+		launch_k1(dev, 1, g, stream);
+		k1_pending = false;
+		update_pending = false;
+		k2_valid = false;
+	}
+
+	void run_k2()
+	{
+		launch_k2(dev, 1, g, stream);
+		k2_valid = true;
+	}
+
+	void ensure_current()
+	{
+		if (k1_pending || update_pending)
+			run_k1();
+		if (!k2_valid)
+			run_k2();
+	}
+};
+
+namespace
+{
+
+template <typename Fn>
+int guarded(Fn &&fn)
+{
+	try
+	{
+		return fn();
+	}
+	catch (const CudaFailure &f)
+	{
+		set_error(f.what());
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+	catch (const std::bad_alloc &)
+	{
+		set_error("host allocation failed");
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+	catch (const std::exception &ex)
+	{
+		set_error(ex.what());
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+}
+
+bool device_present()
+{
+	int count = 0;
+	if (cudaGetDeviceCount(&count) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return false;
+	}
+	return count > 0;
+}
+
+} // namespace
+
+extern "C" {
+
+const char *bgt_gpu_last_error(void) { return g_last_error.c_str(); }
+
+uint64_t bgt_gpu_kernel_launch_count(void) { return g_launches.load(); }
+
+int bgt_cuda_provider_available(void) { return device_present() ? 1 : 0; }
+
+int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const double *prior, int precision,
+						   bgt_gpu_lattice **out)
+{
+	if (out == nullptr || prior == nullptr)
+	{
+		set_error("null output or prior pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	*out = nullptr;
+	std::string why;
+	if (const int rc = check_supported(subjects, variants, &why))
+	{
+		set_error(why);
+		return rc;
+	}
+	if (lattice_type != 0 && lattice_type != 1)
+	{
+		set_error("lattice type must be 0 (non-dilution) or 1 (dilution)");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (precision != BGT_GPU_FP64)
+	{
+		set_error("only FP64 lattices are supported by this build");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (!device_present())
+	{
+		set_error("no CUDA device");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return guarded([&]() -> int {
+		configure_kernels();
+		auto *lat = new bgt_gpu_lattice();
+		try
+		{
+			lat->g = make_geometry(subjects, variants);
+			lat->dilution = lattice_type;
+			lat->precision = precision;
+			const LatticeGeometry &g = lat->g;
+			cuda_check(cudaStreamCreateWithFlags(&lat->own_stream, cudaStreamNonBlocking), "stream create");
+			lat->stream = lat->own_stream;
+			const size_t states = size_t{1} << g.atoms;
+			const size_t rows = size_t{1} << g.hbits;
+			cuda_check(cudaMalloc(&lat->dev, sizeof(LatticeDev)), "alloc state");
+			cuda_check(cudaMalloc(&lat->q, states * sizeof(double)), "alloc posterior");
+			cuda_check(cudaMalloc(&lat->m1, static_cast<size_t>(g.nblk) * rows * kColW * sizeof(unsigned long long)),
+					   "alloc zeta partials");
+			cuda_check(cudaMalloc(&lat->tile_total, rows * sizeof(unsigned long long)), "alloc tile totals");
+			cuda_check(cudaMalloc(&lat->tile_scale, rows * sizeof(int)), "alloc tile scales");
+			cuda_check(cudaMalloc(&lat->blk_score, g.nblk * sizeof(unsigned long long)), "alloc block scores");
+			cuda_check(cudaMalloc(&lat->blk_e, g.nblk * sizeof(unsigned int)), "alloc block winners");
+			cuda_check(cudaMalloc(&lat->dil, static_cast<size_t>(subjects) * (subjects + 1) * sizeof(double)),
+					   "alloc dilution");
+			cuda_check(cudaMalloc(&lat->prior_lo, (size_t{1} << g.tbits) * sizeof(double)), "alloc prior lo");
+			cuda_check(cudaMalloc(&lat->prior_hi, rows * sizeof(double)), "alloc prior hi");
+			cuda_check(cudaMalloc(&lat->pi0, g.atoms * sizeof(double)), "alloc pi0");
+			cuda_check(cudaMalloc(&lat->scratch_u64, 64 * sizeof(unsigned long long)), "alloc scratch");
+			cuda_check(cudaMemcpyAsync(lat->pi0, prior, g.atoms * sizeof(double), cudaMemcpyHostToDevice, lat->stream),
+					   "prior upload");
+			const unsigned int span = std::max<unsigned int>(1u << g.tbits, static_cast<unsigned int>(rows));
+			prior_tables<<<(span + 255) / 256, 256, 0, lat->stream>>>(lat->pi0, g.atoms, g.tbits, lat->prior_lo,
+																		lat->prior_hi);
+			cuda_check(cudaGetLastError(), "prior tables launch");
+			count_launches(1);
+			LatticeDev &h = lat->host;
+			std::memset(&h, 0, sizeof(h));
+			h.n = subjects;
+			h.k = variants;
+			h.atoms = g.atoms;
+			h.tbits = g.tbits;
+			h.hbits = g.hbits;
+			h.nblk = g.nblk;
+			h.dilution = lattice_type;
+			h.orig_n = subjects;
+			h.q_in = lat->q;
+			h.q_out = lat->q;
+			h.m1 = lat->m1;
+			h.tile_total = lat->tile_total;
+			h.tile_scale = lat->tile_scale;
+			h.blk_score = lat->blk_score;
+			h.blk_e = lat->blk_e;
+			h.dil = lat->dil;
+			h.prior_lo = lat->prior_lo;
+			h.prior_hi = lat->prior_hi;
+			h.mode = kGenerate;
+			h.z_norm = 1.0;
+			h.active = g.n >= 32 ? 0xFFFFFFFFu : ((1u << g.n) - 1u);
+			cuda_check(cudaMemcpyAsync(lat->dev, &h, sizeof(h), cudaMemcpyHostToDevice, lat->stream), "state upload");
+			lat->run_k1();
+			cuda_check(cudaStreamSynchronize(lat->stream), "create sync");
+			lat->check_device_error();
+		}
+		catch (...)
+		{
+			delete lat;
+			throw;
+		}
+		*out = lat;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_destroy(bgt_gpu_lattice *lattice)
+{
+	if (lattice)
+	{
+		cudaStreamSynchronize(lattice->stream);
+		delete lattice;
+	}
+	return BGT_GPU_OK;
+}
+
+int bgt_gpu_lattice_set_stream(bgt_gpu_lattice *lattice, void *stream)
+{
+	if (!lattice)
+		return BGT_GPU_MISSING_DILUTION;
+	return guarded([&]() -> int {
+		cuda_check(cudaStreamSynchronize(lattice->stream), "stream switch sync");
+		lattice->stream = stream ? static_cast<cudaStream_t>(stream) : lattice->own_stream;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_select(bgt_gpu_lattice *lattice, int selector, uint32_t *experiment)
+{
+	if (!lattice || !experiment)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	const int resolved = selector == 0 ? (lattice->g.k == 1 ? 1 : 2) : selector;
+	if (resolved != 1 && resolved != 2)
+	{
+		set_error("unsupported selector");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (resolved == 1 && lattice->g.k != 1)
+	{
+		set_error("Op-BHA experiment selection is only supported for binary lattices.");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return guarded([&]() -> int {
+		lattice->ensure_current();
+		*experiment = lattice->get_field<unsigned int>(offsetof(LatticeDev, best_e));
+		lattice->check_device_error();
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_reselect(bgt_gpu_lattice *lattice, int selector, uint32_t *experiment)
+{
+	if (!lattice || !experiment)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return guarded([&]() -> int {
+		if (!lattice->update_pending)
+			lattice->k1_pending = true;
+		lattice->k2_valid = false;
+		return bgt_gpu_lattice_select(lattice, selector, experiment);
+	});
+}
+
+int bgt_gpu_lattice_update(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
+						   const double *const *dilution_rows)
+{
+	if (!lattice)
+	{
+		set_error("null lattice");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (lattice->dilution && dilution_rows == nullptr && !lattice->have_dilution)
+	{
+		set_error("dilution table is required for dilution models.");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return guarded([&]() -> int {
+		if (lattice->update_pending || lattice->k1_pending)
+			lattice->run_k1();
+		if (lattice->dilution && dilution_rows != nullptr)
+		{
+			const std::vector<double> flat = flatten_dilution(dilution_rows, lattice->g.n);
+			cuda_check(cudaMemcpyAsync(lattice->dil, flat.data(), flat.size() * sizeof(double), cudaMemcpyHostToDevice,
+									   lattice->stream),
+					   "dilution upload");
+			cuda_check(cudaStreamSynchronize(lattice->stream), "dilution upload sync");
+			lattice->have_dilution = true;
+		}
+		const unsigned int subject_mask = lattice->g.n >= 32 ? 0xFFFFFFFFu : ((1u << lattice->g.n) - 1u);
+		lattice->set_field(offsetof(LatticeDev, pend_e), static_cast<unsigned int>(experiment & subject_mask));
+		lattice->set_field(offsetof(LatticeDev, pend_r), static_cast<unsigned int>(response));
+		lattice->set_field(offsetof(LatticeDev, mode), static_cast<int>(kUpdate));
+		lattice->update_pending = true;
+		lattice->k2_valid = false;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_atom_masses(bgt_gpu_lattice *lattice, double *out)
+{
+	if (!lattice || !out)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return guarded([&]() -> int {
+		lattice->ensure_current();
+		unsigned long long fixed[32];
+		cuda_check(cudaMemcpyAsync(fixed, reinterpret_cast<char *>(lattice->dev) + offsetof(LatticeDev, atom_fixed),
+								   sizeof(fixed), cudaMemcpyDeviceToHost, lattice->stream),
+				   "atom mass read");
+		const unsigned long long zg = lattice->get_field<unsigned long long>(offsetof(LatticeDev, z_g));
+		lattice->check_device_error();
+		const double z = static_cast<double>(zg);
+		for (int i = 0; i < lattice->g.atoms; i++)
+			out[i] = static_cast<double>(fixed[i]) / z;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_classify(bgt_gpu_lattice *lattice, double threshold_up, double threshold_lo,
+							 uint32_t *positive_mask, uint32_t *negative_mask)
+{
+	if (!lattice)
+	{
+		set_error("null lattice");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	double masses[32];
+	const int rc = bgt_gpu_lattice_atom_masses(lattice, masses);
+	if (rc != 0)
+		return rc;
+	// update_metadata, src/core/model/lattice_base.cpp:246-264.
+	for (int i = 0; i < lattice->g.atoms; i++)
+	{
+		const uint32_t bit = 1u << i;
+		if ((lattice->pos | lattice->neg) & bit)
+			continue;
+		if (masses[i] < threshold_lo)
+			lattice->pos |= bit;
+		else if (masses[i] > (1 - threshold_up))
+			lattice->neg |= bit;
+	}
+	if (positive_mask)
+		*positive_mask = lattice->pos;
+	if (negative_mask)
+		*negative_mask = lattice->neg;
+	return BGT_GPU_OK;
+}
+
+int bgt_gpu_lattice_read_posterior(bgt_gpu_lattice *lattice, double *out)
+{
+	if (!lattice || !out)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return guarded([&]() -> int {
+		if (lattice->update_pending || lattice->k1_pending)
+			lattice->run_k1();
+		const size_t states = size_t{1} << lattice->g.atoms;
+		cuda_check(cudaMemcpyAsync(out, lattice->q, states * sizeof(double), cudaMemcpyDeviceToHost, lattice->stream),
+				   "posterior read");
+		const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
+		lattice->check_device_error();
+		if (z != 1.0)
+			for (size_t s = 0; s < states; s++)
+				out[s] = out[s] / z;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_posterior_probability(bgt_gpu_lattice *lattice, uint32_t state, double *out)
+{
+	if (!lattice || !out)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (lattice->g.atoms < 32 && (state >> lattice->g.atoms) != 0)
+	{
+		set_error("state index out of range");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return guarded([&]() -> int {
+		if (lattice->update_pending || lattice->k1_pending)
+			lattice->run_k1();
+		double v = 0.0;
+		cuda_check(cudaMemcpyAsync(&v, lattice->q + state, sizeof(double), cudaMemcpyDeviceToHost, lattice->stream),
+				   "posterior read");
+		const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
+		*out = v / z;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, double *out)
+{
+	if (!lattice || !out)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return guarded([&]() -> int {
+		if (lattice->update_pending || lattice->k1_pending)
+			lattice->run_k1();
+		cuda_check(cudaMemsetAsync(lattice->scratch_u64, 0, sizeof(unsigned long long), lattice->stream), "memset");
+		upset_mass_kernel<<<304, 256, 0, lattice->stream>>>(lattice->dev, experiment, lattice->scratch_u64);
+		cuda_check(cudaGetLastError(), "upset mass launch");
+		count_launches(1);
+		unsigned long long m = 0;
+		cuda_check(cudaMemcpyAsync(&m, lattice->scratch_u64, sizeof(m), cudaMemcpyDeviceToHost, lattice->stream),
+				   "upset mass read");
+		const int s_g = lattice->get_field<int>(offsetof(LatticeDev, s_g));
+		const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
+		*out = std::ldexp(static_cast<double>(m), -s_g) / z;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, double alpha, double h,
+						double threshold_up, double threshold_lo, uint64_t seed, uint64_t session,
+						uint32_t true_state, uint32_t *experiments, uint32_t *responses, uint32_t *positive_masks,
+						uint32_t *negative_masks)
+{
+	if (!lattice)
+	{
+		set_error("null lattice");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (stages < 0)
+	{
+		set_error("stages must be non-negative");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	const int resolved = selector == 0 ? (lattice->g.k == 1 ? 1 : 2) : selector;
+	if (resolved == 1 && lattice->g.k != 1)
+	{
+		set_error("Op-BHA experiment selection is only supported for binary lattices.");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return guarded([&]() -> int {
+		if (stages == 0)
+			return BGT_GPU_OK;
+		if (stages > lattice->sess_capacity)
+		{
+			cudaFree(lattice->sess_out);
+			lattice->sess_out = nullptr;
+			cuda_check(cudaMalloc(&lattice->sess_out, 4 * static_cast<size_t>(stages) * sizeof(unsigned int)),
+					   "alloc session outputs");
+			lattice->sess_capacity = stages;
+		}
+		if (lattice->dilution)
+		{
+			std::vector<double> flat(static_cast<size_t>(lattice->g.n) * (lattice->g.n + 1), 0.0);
+			for (int L = 1; L <= lattice->g.n; L++)
+			{
+				flat[static_cast<size_t>(L - 1) * (lattice->g.n + 1)] = alpha;
+				for (int r = 1; r <= L; r++)
+				{
+					const int kk = L - r;
+					flat[static_cast<size_t>(L - 1) * (lattice->g.n + 1) + r] = 1 - alpha * r / (kk * h + r);
+				}
+			}
+			cuda_check(cudaMemcpyAsync(lattice->dil, flat.data(), flat.size() * sizeof(double), cudaMemcpyHostToDevice,
+									   lattice->stream),
+					   "dilution upload");
+			cuda_check(cudaStreamSynchronize(lattice->stream), "dilution sync");
+			lattice->have_dilution = true;
+		}
+		if (lattice->update_pending || lattice->k1_pending)
+			lattice->run_k1();
+		unsigned int *o = lattice->sess_out;
+		const size_t S = static_cast<size_t>(stages);
+		LatticeDev &hst = lattice->host;
+		hst.sess_active = 1;
+		hst.stage = 0;
+		hst.stages = stages;
+		hst.alpha = alpha;
+		hst.hpar = h;
+		hst.up = threshold_up;
+		hst.lo = threshold_lo;
+		hst.seed = seed;
+		hst.session = session;
+		hst.truth = true_state;
+		hst.out_e = o;
+		hst.out_r = o + S;
+		hst.out_pos = o + 2 * S;
+		hst.out_neg = o + 3 * S;
+		const size_t first = offsetof(LatticeDev, sess_active);
+		const size_t last = offsetof(LatticeDev, out_neg) + sizeof(unsigned int *);
+		cuda_check(cudaMemcpyAsync(reinterpret_cast<char *>(lattice->dev) + first,
+								   reinterpret_cast<const char *>(&hst) + first, last - first, cudaMemcpyHostToDevice,
+								   lattice->stream),
+				   "session setup");
+		lattice->set_field(offsetof(LatticeDev, pos), lattice->pos);
+		lattice->set_field(offsetof(LatticeDev, neg), lattice->neg);
+		lattice->set_field(offsetof(LatticeDev, classify_on_update), 1);
+		// Stage loop: K2 selects and queues the update, K1 applies it and classifies.
+		for (int s = 0; s < stages; s++)
+		{
+			launch_k2(lattice->dev, 1, lattice->g, lattice->stream);
+			launch_k1(lattice->dev, 1, lattice->g, lattice->stream);
+		}
+		lattice->set_field(offsetof(LatticeDev, classify_on_update), 0);
+		lattice->k1_pending = false;
+		lattice->update_pending = false;
+		lattice->k2_valid = false;
+		std::vector<unsigned int> host(4 * S);
+		cuda_check(cudaMemcpyAsync(host.data(), o, host.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+								   lattice->stream),
+				   "session read");
+		cuda_check(cudaStreamSynchronize(lattice->stream), "session sync");
+		lattice->check_device_error();
+		lattice->pos = host[2 * S + S - 1];
+		lattice->neg = host[3 * S + S - 1];
+		if (experiments)
+			std::memcpy(experiments, host.data(), S * sizeof(uint32_t));
+		if (responses)
+			std::memcpy(responses, host.data() + S, S * sizeof(uint32_t));
+		if (positive_masks)
+			std::memcpy(positive_masks, host.data() + 2 * S, S * sizeof(uint32_t));
+		if (negative_masks)
+			std::memcpy(negative_masks, host.data() + 3 * S, S * sizeof(uint32_t));
+		return BGT_GPU_OK;
+	});
+}
+
+} // extern "C"

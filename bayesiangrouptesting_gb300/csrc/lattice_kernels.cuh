@@ -1,0 +1,201 @@
+// Device side of the GB300 lattice provider: per-lattice state and the two
+// kernels that make up one lattice stage.
+//
+// The posterior of a lattice with A = subjects * variants atoms is an array of
+// 2^A FP64 values q[s] stored unnormalised together with its normaliser
+// Z_norm (the reader's posterior is q[s] / Z_norm; Z_norm = 1 for the raw
+// product prior, as in src/core/model/lattice_base.cpp:184-208).
+//
+// GB300 runs FP64 at about 0.5 T add/s but moves ~0.8 G doubles per
+// microsecond from HBM, so every reduction on this path -- the normalising
+// sum of Lattice::update (lattice_base.cpp:230-244), the atom marginals
+// (lattice_base.cpp:25-41) and the subset zeta transform behind Op-BHA /
+// Op-BBPA (src/kernels/cpu/bbpa.cpp:497-512) -- is done in exact unsigned
+// 64-bit fixed point on the integer pipes.  Each element costs at most one
+// FP64 multiply (the likelihood factor).  Because integer addition is exact
+// and associative, the zeta levels may run in any order and any tiling and the
+// result is bit-identical run to run; the only rounding is the one conversion
+// of each input to fixed point.
+//
+// Stage structure for one binary (k = 1) lattice of n subjects, N = 2^n:
+//   K1 zeta_low   one CTA per tile of 2^t states (t = min(n, 14)):
+//                 [apply pending update q *= L/Z] -> q (FP64, written back)
+//                 -> u64 at a per-tile scale -> zeta over the t low bits
+//                 -> column-block-major partial sums M1 + tile totals.
+//                 The last CTA to finish derives the global scale and the
+//                 exact fixed-point total Z_g.
+//                 It also forms the exact atom marginals (low atoms from the
+//                 singleton columns of M1, high atoms from the tile totals)
+//                 and, after an update, classifies the atoms.
+//   K2 zeta_high  one CTA per 16-column block of M1: rescale to the global
+//                 scale, zeta over the h = n - t high bits, exact score
+//                 |2 M(E) - Z_g| (Op-BHA; Op-BBPA for k = 1 is the same
+//                 ordering in exact arithmetic) over the experiments inside
+//                 the active-subject mask, argmin with the lowest index on
+//                 ties (bbpa.cpp:537-551).  The last CTA reduces the block
+//                 winners and, in session mode, draws the response and queues
+//                 the next update.
+#pragma once
+
+#include <cstdint>
+
+#include "bgt_session_rng.h"
+
+namespace bgt_gpu
+{
+
+constexpr int kTileBits = 14;                 // states per K1 tile = 2^14
+constexpr int kTileThreads = 1024;            // 16 states per thread
+constexpr int kPerThread = (1 << kTileBits) / kTileThreads;
+constexpr int kColW = 16;                     // K2 column block: 16 u64 = 128 B per row
+constexpr int kMaxHighBits = 10;              // K2 holds up to 2^10 rows x 16 columns (128 KB)
+constexpr int kHighThreads = 512;
+constexpr int kMaxAtoms = 30;
+constexpr int kMaxClasses = 32;               // likelihood classes for k = 1 (popcount 0..n)
+
+// Modes of K1.
+enum K1Mode : int
+{
+	kLoad = 0,   // q unchanged: only the zeta partial sums
+	kUpdate = 1, // q_out = q_in * L(class)/Z_norm
+	kGenerate = 2 // q_out = prior_hi[row] * prior_lo[col]
+};
+
+struct LatticeDev
+{
+	// ---- geometry (host-set) ----
+	int n;        // current subjects
+	int k;        // variants
+	int atoms;    // n * k
+	int tbits;    // low bits handled in K1 tiles
+	int hbits;    // high bits handled in K2
+	int nblk;     // K2 column blocks (max(1, 2^tbits / 16))
+	int dilution; // 0 / 1
+	int orig_n;   // subjects of the dilution table
+	// ---- buffers (host-set) ----
+	const double *q_in;
+	double *q_out;
+	unsigned long long *m1;        // [nblk][2^hbits][16]
+	unsigned long long *tile_total; // [2^hbits]
+	int *tile_scale;               // [2^hbits]
+	unsigned long long *blk_score; // [nblk]
+	unsigned int *blk_e;           // [nblk]
+	const double *dil;             // [orig_n][orig_n + 1]
+	const double *prior_lo;        // [2^tbits]
+	const double *prior_hi;        // [2^hbits]
+	// ---- dynamic (device-updated) ----
+	int mode;                      // K1Mode for the next K1
+	unsigned int pend_e, pend_r;   // pending update
+	double z_norm;                 // normaliser of q
+	int s_g;                       // global fixed-point scale (value * 2^s_g)
+	unsigned long long z_g;        // exact fixed-point total at scale s_g
+	unsigned int active;           // candidate experiments are subsets of this mask
+	unsigned int best_e;
+	unsigned long long best_score;
+	unsigned long long atom_fixed[32];
+	unsigned int pos, neg;         // classification masks (internal order)
+	int classify_on_update;        // K1 classifies after applying an update (tree/session)
+	int skip;                      // K2 leaves this lattice alone (tree leaves)
+	int error;                     // nonzero: a kernel detected a failure
+	unsigned int k1_count, k2_count; // last-CTA counters (reset by the last CTA)
+	// ---- session (device-driven loop) ----
+	int sess_active;
+	int stage, stages;
+	double alpha, hpar, up, lo;
+	unsigned long long seed, session;
+	unsigned int truth;
+	unsigned int *out_e, *out_r, *out_pos, *out_neg;
+};
+
+enum LatticeError : int
+{
+	kErrNone = 0,
+	kErrZeroMass = 1,   // normalising constant is zero
+	kErrNonFinite = 2   // a non-finite posterior value was seen
+};
+
+// ------------------------------------------------------------------ helpers
+
+__device__ __forceinline__ unsigned int tile_swz(unsigned int x) { return x ^ ((x >> 4) & 15u); }
+
+// v * 2^64 truncated to FP32 (never above the true value); 0 when below the
+// FP32 normal range.  Integer-only: no FP64 conversion instruction.
+__device__ __forceinline__ float approx_scaled(double v)
+{
+	const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+	const int e = static_cast<int>(b >> 52) & 0x7FF;
+	const int ef = e - 1023 + 64 + 127;
+	if (ef <= 0)
+		return 0.0f;
+	if (ef >= 255)
+		return 3.0e38f;
+	const unsigned int mf = static_cast<unsigned int>((b >> 29) & 0x7FFFFFull);
+	return __int_as_float((ef << 23) | static_cast<int>(mf));
+}
+
+// round(v * 2^scale) for a finite v >= 0 whose scaled value is below 2^63.
+__device__ __forceinline__ unsigned long long to_fixed(double v, int scale)
+{
+	const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+	const int e = static_cast<int>(b >> 52) & 0x7FF;
+	if (e == 0)
+		return 0ull; // zero or subnormal (below 2^-1022: contributes < 2^-700 of any tile)
+	const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+	const int sh = e - 1075 + scale;
+	if (sh >= 0)
+		return m << (sh > 10 ? 10 : sh);
+	if (sh <= -54)
+		return 0ull;
+	const int rs = -sh;
+	return (m + (1ull << (rs - 1))) >> rs;
+}
+
+// round(v * 2^d) for a fixed-point value v.
+__device__ __forceinline__ unsigned long long rescale(unsigned long long v, int d)
+{
+	if (d >= 0)
+		return v << d;
+	const int rs = -d;
+	if (rs >= 64)
+		return 0ull;
+	return (v >> rs) + ((v >> (rs - 1)) & 1ull);
+}
+
+// 2^-s as a double for |s| < 1000 (built from the exponent field).
+__device__ __host__ __forceinline__ double pow2_neg(int s)
+{
+	const long long bits = static_cast<long long>(1023 - s) << 52;
+#ifdef __CUDA_ARCH__
+	return __longlong_as_double(bits);
+#else
+	double d;
+	__builtin_memcpy(&d, &bits, sizeof(d));
+	return d;
+#endif
+}
+
+// Likelihood of response r for a binary lattice at pool class pc =
+// popcount(e & s) (negatives in the pool), restating
+// ReplicatedNonDilutionLattice / ReplicatedDilutionLattice::response_prob
+// (src/core/model/replicated_lattice.cpp:8-28) for one variant.
+__device__ __forceinline__ double binary_likelihood(int dilution, int pool, int pc, unsigned int r, const double *dil,
+												   int dil_stride)
+{
+	if (!dilution)
+	{
+		const double negative_response = BGT_NON_DILUTION_NEGATIVE;
+		const bool contained = pc == pool;
+		return contained ? ((r & 1u) == 0 ? (1.0 - negative_response) : negative_response)
+						 : ((r & 1u) == 0 ? negative_response : (1.0 - negative_response));
+	}
+	const int col = pool - pc;
+	const double p = pool == 0 ? dil[0] : dil[(pool - 1) * dil_stride + col];
+	return (r & 1u) != 0 ? p : 1.0 - p;
+}
+
+__device__ __forceinline__ bool better(unsigned long long s, unsigned int e, unsigned long long bs, unsigned int be)
+{
+	return s < bs || (s == bs && e < be);
+}
+
+} // namespace bgt_gpu

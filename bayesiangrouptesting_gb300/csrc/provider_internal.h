@@ -1,0 +1,38 @@
+// Shared host-side declarations of the GB300 lattice provider.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace bgt_gpu
+{
+
+struct LatticeDev;
+
+// A CUDA call failed or a kernel reported an error; mapped to status 4 at the
+// C ABI (the reference's BGT_CUDA_CHECK, include/bgt/detail/cuda_checks.hpp).
+struct CudaFailure : std::runtime_error
+{
+	explicit CudaFailure(const std::string &what) : std::runtime_error(what) {}
+};
+
+struct LatticeGeometry
+{
+	int n = 0, k = 1, atoms = 0, tbits = 0, hbits = 0, nblk = 1;
+};
+
+void set_error(const std::string &message);
+void count_launches(uint64_t n);
+void cuda_check(cudaError_t err, const char *what);
+void configure_kernels();
+LatticeGeometry make_geometry(int n, int k);
+int check_supported(int subjects, int variants, std::string *why);
+void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
+void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
+size_t k1_smem_bytes();
+size_t k2_smem_bytes(int hbits);
+
+} // namespace bgt_gpu

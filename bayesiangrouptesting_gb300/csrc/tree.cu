@@ -1,0 +1,620 @@
+// Device tree simulation: the GB300 replacement of bgt_cuda_provider_run
+// (reference src/kernels/cuda/cuda_provider.cu:2371-2445), with the CPU
+// provider's semantics (src/runtime/simulation_runner.cpp:92-132,
+// src/core/tree/global_tree_intra.cpp:8-40, src/core/tree/tree.cpp:70-199).
+//
+// Build: level-synchronous.  All nodes of one depth are one batch: a single
+// K1 launch applies every child's update (reading its parent's posterior)
+// and classifies it, a single K2 launch selects every non-leaf node's next
+// experiment.  Classified subjects are masked out of the candidate set
+// instead of being marginalised out; the candidate order and the zeta values
+// on the remaining subjects are those of the reference's shrunk lattice
+// (Tree::true_ex, tree.cpp:55-68, maps the compact choice back to the same
+// experiment).
+//
+// Sweep: one thread per true state walks the tree in preorder, multiplying
+// branch probabilities (apply_true_state_helper, tree.cpp:174-199) and
+// accumulating the leaf statistics of Tree::parse (tree.cpp:70-111) in
+// registers; blocks reduce to per-block partials, summed in a fixed order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "bgt_gpu.h"
+#include "lattice_kernels.cuh"
+#include "provider_internal.h"
+
+namespace bgt_gpu
+{
+
+__global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
+
+constexpr int kSweepThreads = 256;
+constexpr int kMaxTreeNodes = 4096; // preorder nodes held in shared memory
+constexpr int kMaxDepth = 30;
+
+struct SweepNode
+{
+	unsigned int ex;
+	unsigned int res;
+	unsigned int neg;
+	unsigned int pos;
+	int stage;
+	int end;        // preorder index just past this node's subtree
+	int leaf;       // 1 for a leaf
+	int classified; // leaf is fully classified
+};
+
+struct SweepParams
+{
+	int atoms, subjects, variants, dilution, count;
+	double thres;
+	const double *pi0;
+	const double *dil; // [subjects][subjects + 1]
+	const SweepNode *nodes;
+	double *partials;  // [gridDim.x][7]
+};
+
+// One variant's likelihood factor, restating response_prob
+// (src/core/model/replicated_lattice.cpp:8-28) on the original lattice.
+__device__ __forceinline__ double edge_factor(const SweepParams &p, unsigned int e, unsigned int r, unsigned int t)
+{
+	double ret = 1.0;
+	const int pool = __popc(e);
+	for (int v = 0; v < p.variants; v++)
+	{
+		const unsigned int shifted = static_cast<unsigned int>(static_cast<unsigned long long>(t) >> (v * p.subjects));
+		const int pc = __popc(e & shifted);
+		ret *= binary_likelihood(p.dilution, pool, pc, (r >> v) & 1u, p.dil, p.subjects + 1);
+	}
+	return ret;
+}
+
+__global__ void __launch_bounds__(kSweepThreads) tree_sweep(SweepParams p)
+{
+	extern __shared__ SweepNode nodes[];
+	for (int i = threadIdx.x; i < p.count; i += blockDim.x)
+		nodes[i] = p.nodes[i];
+	__syncthreads();
+	double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+	const unsigned long long total = 1ull << p.atoms;
+	double lvl[kMaxDepth + 2];
+	for (unsigned long long ts = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; ts < total;
+		 ts += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+	{
+		const unsigned int t = static_cast<unsigned int>(ts);
+		// prior_prob (src/core/model/lattice_base.cpp:197-208) of the true state.
+		double coef = 1.0;
+		for (int a = 0; a < p.atoms; a++)
+			coef *= (t & (1u << a)) ? (1.0 - p.pi0[a]) : p.pi0[a];
+		coef = coef * 1.0;
+		double correct = 0, incorrect = 0, fp = 0, fn = 0, unclas = 0, exp_stage = 0, exp_test = 0;
+		lvl[0] = 1.0;
+		int i = 0;
+		while (i < p.count)
+		{
+			const SweepNode &nd = nodes[i];
+			double bp;
+			if (i == 0)
+			{
+				bp = 1.0;
+			}
+			else
+			{
+				bp = lvl[nd.stage - 1] * edge_factor(p, nd.ex, nd.res, t);
+				if (!(bp > p.thres))
+				{
+					i = nd.end;
+					continue;
+				}
+			}
+			lvl[nd.stage] = bp;
+			if (nd.leaf)
+			{
+				if (bp >= p.thres)
+				{
+					const int index = nd.stage;
+					if (nd.classified && nd.neg == t)
+					{
+						correct += bp * coef;
+					}
+					else if (nd.classified)
+					{
+						const double total_positive = static_cast<double>(__popc(nd.pos));
+						const double total_negative = static_cast<double>(__popc(nd.neg));
+						const double fpv =
+							total_positive == 0.0 ? 0.0 : __popc((nd.neg ^ t) & t) / total_positive;
+						const double fnv =
+							total_negative == 0.0 ? 0.0 : __popc((nd.neg ^ t) & ~t) / total_negative;
+						incorrect += bp * coef;
+						fp += fpv * coef * bp;
+						fn += fnv * coef * bp;
+					}
+					else
+					{
+						unclas = unclas + bp;
+					}
+					exp_stage = exp_stage + static_cast<double>(index) * bp;
+					exp_test = exp_test + index * bp;
+				}
+			}
+			i++;
+		}
+		acc[0] += correct;
+		acc[1] += incorrect;
+		acc[2] += fp;
+		acc[3] += fn;
+		acc[4] += unclas * coef;
+		acc[5] += exp_stage * coef;
+		acc[6] += exp_test * coef;
+	}
+	// Block reduction (fixed order: warp shuffles, then warps in index order).
+	__shared__ double red[kSweepThreads / 32][7];
+	for (int j = 0; j < 7; j++)
+	{
+		double v = acc[j];
+		for (int o = 16; o > 0; o >>= 1)
+			v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+		if ((threadIdx.x & 31) == 0)
+			red[threadIdx.x >> 5][j] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x < 7)
+	{
+		double v = 0.0;
+		for (int w = 0; w < kSweepThreads / 32; w++)
+			v += red[w][threadIdx.x];
+		p.partials[blockIdx.x * 7 + threadIdx.x] = v;
+	}
+}
+
+namespace
+{
+
+struct HostNode
+{
+	unsigned int ex = 0, res = 0;
+	int stage = 0;
+	unsigned int pos = 0, neg = 0;
+	bool leaf = false;
+	int children[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+	int nchildren = 0;
+};
+
+struct Level
+{
+	std::vector<int> nodes;       // host node ids
+	LatticeDev *states = nullptr; // device array, one per node
+	double *q = nullptr;          // posteriors, one 2^A slice per node
+	unsigned long long *m1 = nullptr;
+	unsigned long long *tile_total = nullptr;
+	int *tile_scale = nullptr;
+	unsigned long long *blk_score = nullptr;
+	unsigned int *blk_e = nullptr;
+	std::vector<LatticeDev> host;
+
+	void release()
+	{
+		cudaFree(states);
+		cudaFree(q);
+		cudaFree(m1);
+		cudaFree(tile_total);
+		cudaFree(tile_scale);
+		cudaFree(blk_score);
+		cudaFree(blk_e);
+		states = nullptr;
+		q = nullptr;
+		m1 = nullptr;
+		tile_total = nullptr;
+		tile_scale = nullptr;
+		blk_score = nullptr;
+		blk_e = nullptr;
+	}
+};
+
+struct DeviceBuffer
+{
+	void *ptr = nullptr;
+	~DeviceBuffer() { cudaFree(ptr); }
+};
+
+void allocate_level(Level &lv, const LatticeGeometry &g)
+{
+	const size_t count = lv.nodes.size();
+	const size_t states = size_t{1} << g.atoms;
+	const size_t rows = size_t{1} << g.hbits;
+	cuda_check(cudaMalloc(&lv.states, count * sizeof(LatticeDev)), "alloc tree states");
+	cuda_check(cudaMalloc(&lv.q, count * states * sizeof(double)), "alloc tree posteriors");
+	cuda_check(cudaMalloc(&lv.m1, count * static_cast<size_t>(g.nblk) * rows * kColW * sizeof(unsigned long long)),
+			   "alloc tree zeta partials");
+	cuda_check(cudaMalloc(&lv.tile_total, count * rows * sizeof(unsigned long long)), "alloc tile totals");
+	cuda_check(cudaMalloc(&lv.tile_scale, count * rows * sizeof(int)), "alloc tile scales");
+	cuda_check(cudaMalloc(&lv.blk_score, count * g.nblk * sizeof(unsigned long long)), "alloc block scores");
+	cuda_check(cudaMalloc(&lv.blk_e, count * g.nblk * sizeof(unsigned int)), "alloc block winners");
+	lv.host.assign(count, LatticeDev{});
+}
+
+void bind_level_buffers(Level &lv, const LatticeGeometry &g, size_t i, LatticeDev &d)
+{
+	const size_t states = size_t{1} << g.atoms;
+	const size_t rows = size_t{1} << g.hbits;
+	d.q_out = lv.q + i * states;
+	d.m1 = lv.m1 + i * static_cast<size_t>(g.nblk) * rows * kColW;
+	d.tile_total = lv.tile_total + i * rows;
+	d.tile_scale = lv.tile_scale + i * rows;
+	d.blk_score = lv.blk_score + i * g.nblk;
+	d.blk_e = lv.blk_e + i * g.nblk;
+}
+
+void flatten_preorder(const std::vector<HostNode> &tree, int node, std::vector<SweepNode> &out, int atoms)
+{
+	const HostNode &h = tree[static_cast<size_t>(node)];
+	const int idx = static_cast<int>(out.size());
+	SweepNode s{};
+	s.ex = h.ex;
+	s.res = h.res;
+	s.pos = h.pos;
+	s.neg = h.neg;
+	s.stage = h.stage;
+	s.leaf = h.nchildren == 0 ? 1 : 0;
+	s.classified = __builtin_popcount(h.pos | h.neg) == atoms ? 1 : 0;
+	out.push_back(s);
+	for (int c = 0; c < h.nchildren; c++)
+		flatten_preorder(tree, h.children[c], out, atoms);
+	out[static_cast<size_t>(idx)].end = static_cast<int>(out.size());
+}
+
+} // namespace
+
+// Builds the tree and evaluates TreeStats; throws CudaFailure on error.
+// Returns a status when the request is unsupported.
+int run_tree(int use_dilution, int subjects, int variants, const double *prior, int search_depth, double up, double lo,
+			 double branch_threshold, int selector, const std::vector<double> &dil_flat, bgt_tree_stats *stats)
+{
+	const LatticeGeometry g = make_geometry(subjects, variants);
+	configure_kernels();
+	cudaStream_t stream = nullptr;
+	cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "tree stream");
+	struct StreamGuard
+	{
+		cudaStream_t s;
+		~StreamGuard() { cudaStreamDestroy(s); }
+	} sg{stream};
+	(void)selector;
+
+	DeviceBuffer d_pi0, d_dil, d_lo, d_hi;
+	const size_t rows = size_t{1} << g.hbits;
+	cuda_check(cudaMalloc(&d_pi0.ptr, g.atoms * sizeof(double)), "alloc pi0");
+	cuda_check(cudaMalloc(&d_dil.ptr, std::max<size_t>(1, dil_flat.size()) * sizeof(double)), "alloc dilution");
+	cuda_check(cudaMalloc(&d_lo.ptr, (size_t{1} << g.tbits) * sizeof(double)), "alloc prior lo");
+	cuda_check(cudaMalloc(&d_hi.ptr, rows * sizeof(double)), "alloc prior hi");
+	cuda_check(cudaMemcpyAsync(d_pi0.ptr, prior, g.atoms * sizeof(double), cudaMemcpyHostToDevice, stream), "pi0 up");
+	if (!dil_flat.empty())
+		cuda_check(cudaMemcpyAsync(d_dil.ptr, dil_flat.data(), dil_flat.size() * sizeof(double),
+								   cudaMemcpyHostToDevice, stream),
+				   "dilution up");
+	{
+		const unsigned int span = std::max<unsigned int>(1u << g.tbits, static_cast<unsigned int>(rows));
+		prior_tables<<<(span + 255) / 256, 256, 0, stream>>>(static_cast<double *>(d_pi0.ptr), g.atoms, g.tbits,
+															 static_cast<double *>(d_lo.ptr),
+															 static_cast<double *>(d_hi.ptr));
+		cuda_check(cudaGetLastError(), "prior tables");
+		count_launches(1);
+	}
+
+	const unsigned int subject_mask = subjects >= 32 ? 0xFFFFFFFFu : ((1u << subjects) - 1u);
+	const int R = 1 << variants;
+	std::vector<HostNode> tree(1);
+	Level cur;
+	cur.nodes.push_back(0);
+	allocate_level(cur, g);
+	{
+		LatticeDev &d = cur.host[0];
+		d.n = subjects;
+		d.k = variants;
+		d.atoms = g.atoms;
+		d.tbits = g.tbits;
+		d.hbits = g.hbits;
+		d.nblk = g.nblk;
+		d.dilution = use_dilution;
+		d.orig_n = subjects;
+		d.dil = static_cast<double *>(d_dil.ptr);
+		d.prior_lo = static_cast<double *>(d_lo.ptr);
+		d.prior_hi = static_cast<double *>(d_hi.ptr);
+		bind_level_buffers(cur, g, 0, d);
+		d.q_in = d.q_out;
+		d.mode = kGenerate;
+		d.z_norm = 1.0;
+		d.active = subject_mask;
+		d.up = up;
+		d.lo = lo;
+		d.classify_on_update = 1;
+	}
+	Level prev;
+	for (int depth = 0;; depth++)
+	{
+		const size_t count = cur.nodes.size();
+		cuda_check(cudaMemcpyAsync(cur.states, cur.host.data(), count * sizeof(LatticeDev), cudaMemcpyHostToDevice,
+								   stream),
+				   "level states up");
+		launch_k1(cur.states, static_cast<int>(count), g, stream);
+		cuda_check(cudaMemcpyAsync(cur.host.data(), cur.states, count * sizeof(LatticeDev), cudaMemcpyDeviceToHost,
+								   stream),
+				   "level states down");
+		cuda_check(cudaStreamSynchronize(stream), "level K1 sync");
+		prev.release();
+		bool any_internal = false;
+		for (size_t i = 0; i < count; i++)
+		{
+			LatticeDev &d = cur.host[i];
+			if (d.error)
+				throw CudaFailure(d.error == kErrZeroMass ? "posterior normalising constant is zero"
+														  : "non-finite posterior value");
+			HostNode &hn = tree[static_cast<size_t>(cur.nodes[i])];
+			hn.pos = d.pos;
+			hn.neg = d.neg;
+			const bool classified = __builtin_popcount(d.pos | d.neg) == g.atoms;
+			hn.leaf = classified || hn.stage >= search_depth;
+			d.skip = hn.leaf ? 1 : 0;
+			// Candidates: subjects with an unclassified atom (for k = 1, the unclassified atoms).
+			d.active = ~(d.pos | d.neg) & subject_mask;
+			any_internal |= !hn.leaf;
+		}
+		if (!any_internal)
+			break;
+		cuda_check(cudaMemcpyAsync(cur.states, cur.host.data(), count * sizeof(LatticeDev), cudaMemcpyHostToDevice,
+								   stream),
+				   "level states up");
+		launch_k2(cur.states, static_cast<int>(count), g, stream);
+		cuda_check(cudaMemcpyAsync(cur.host.data(), cur.states, count * sizeof(LatticeDev), cudaMemcpyDeviceToHost,
+								   stream),
+				   "level selections down");
+		cuda_check(cudaStreamSynchronize(stream), "level K2 sync");
+		Level next;
+		for (size_t i = 0; i < count; i++)
+		{
+			const int id = cur.nodes[i];
+			if (tree[static_cast<size_t>(id)].leaf)
+				continue;
+			const unsigned int e = cur.host[i].best_e;
+			for (int re = 0; re < R; re++)
+			{
+				HostNode child;
+				child.ex = e;
+				child.res = static_cast<unsigned int>(re);
+				child.stage = tree[static_cast<size_t>(id)].stage + 1;
+				const int cid = static_cast<int>(tree.size());
+				tree.push_back(child);
+				HostNode &parent = tree[static_cast<size_t>(id)];
+				parent.children[parent.nchildren++] = cid;
+				next.nodes.push_back(cid);
+			}
+		}
+		allocate_level(next, g);
+		size_t j = 0;
+		for (size_t i = 0; i < count; i++)
+		{
+			const int id = cur.nodes[i];
+			if (tree[static_cast<size_t>(id)].leaf)
+				continue;
+			const LatticeDev &pd = cur.host[i];
+			for (int re = 0; re < R; re++, j++)
+			{
+				LatticeDev d = pd;
+				bind_level_buffers(next, g, j, d);
+				d.q_in = pd.q_in;
+				d.mode = kUpdate;
+				d.pend_e = pd.best_e;
+				d.pend_r = static_cast<unsigned int>(re);
+				d.skip = 0;
+				d.error = 0;
+				d.k1_count = 0;
+				d.k2_count = 0;
+				next.host[j] = d;
+			}
+		}
+		prev = cur;
+		cur = next;
+		next.states = nullptr;
+		next.q = nullptr;
+		next.m1 = nullptr;
+		next.tile_total = nullptr;
+		next.tile_scale = nullptr;
+		next.blk_score = nullptr;
+		next.blk_e = nullptr;
+	}
+	prev.release();
+	cur.release();
+
+	// Leaf sweep over every true state.
+	std::vector<SweepNode> flat;
+	flatten_preorder(tree, 0, flat, g.atoms);
+	if (flat.size() > static_cast<size_t>(kMaxTreeNodes))
+		throw CudaFailure("tree exceeds the sweep's node capacity");
+	int leaves = 0;
+	for (const SweepNode &s : flat)
+		leaves += s.leaf;
+	DeviceBuffer d_nodes, d_partials;
+	int blocks = 0;
+	cuda_check(cudaDeviceGetAttribute(&blocks, cudaDevAttrMultiProcessorCount, 0), "sm count");
+	const unsigned long long total = 1ull << g.atoms;
+	blocks = static_cast<int>(std::min<unsigned long long>(static_cast<unsigned long long>(blocks) * 8,
+														   (total + kSweepThreads - 1) / kSweepThreads));
+	cuda_check(cudaMalloc(&d_nodes.ptr, flat.size() * sizeof(SweepNode)), "alloc sweep nodes");
+	cuda_check(cudaMalloc(&d_partials.ptr, static_cast<size_t>(blocks) * 7 * sizeof(double)), "alloc partials");
+	cuda_check(cudaMemcpyAsync(d_nodes.ptr, flat.data(), flat.size() * sizeof(SweepNode), cudaMemcpyHostToDevice,
+							   stream),
+			   "sweep nodes up");
+	SweepParams sp;
+	sp.atoms = g.atoms;
+	sp.subjects = subjects;
+	sp.variants = variants;
+	sp.dilution = use_dilution;
+	sp.count = static_cast<int>(flat.size());
+	sp.thres = branch_threshold;
+	sp.pi0 = static_cast<double *>(d_pi0.ptr);
+	sp.dil = static_cast<double *>(d_dil.ptr);
+	sp.nodes = static_cast<SweepNode *>(d_nodes.ptr);
+	sp.partials = static_cast<double *>(d_partials.ptr);
+	const size_t smem = flat.size() * sizeof(SweepNode);
+	if (smem > 48 * 1024)
+		cuda_check(cudaFuncSetAttribute(tree_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
+				   "sweep smem");
+	tree_sweep<<<blocks, kSweepThreads, smem, stream>>>(sp);
+	cuda_check(cudaGetLastError(), "sweep launch");
+	count_launches(1);
+	std::vector<double> partials(static_cast<size_t>(blocks) * 7);
+	cuda_check(cudaMemcpyAsync(partials.data(), d_partials.ptr, partials.size() * sizeof(double),
+							   cudaMemcpyDeviceToHost, stream),
+			   "partials down");
+	cuda_check(cudaStreamSynchronize(stream), "sweep sync");
+	double sums[7] = {0, 0, 0, 0, 0, 0, 0};
+	for (int b = 0; b < blocks; b++)
+		for (int j2 = 0; j2 < 7; j2++)
+			sums[j2] += partials[static_cast<size_t>(b) * 7 + j2];
+	stats->total_leaves = leaves;
+	stats->correct_probability = sums[0];
+	stats->incorrect_probability = sums[1];
+	stats->false_positive_probability = sums[2];
+	stats->false_negative_probability = sums[3];
+	stats->unclassified_probability = sums[4];
+	stats->expected_stages = sums[5];
+	stats->expected_tests = sums[6];
+	return BGT_GPU_OK;
+}
+
+} // namespace bgt_gpu
+
+using namespace bgt_gpu;
+
+extern "C" {
+
+int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const double *prior, int search_depth,
+						  double threshold_up, double threshold_lo, double branch_threshold, int selector,
+						  double **dilution, bgt_tree_stats *stats)
+{
+	if (stats == nullptr)
+	{
+		set_error("null stats pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	*stats = bgt_tree_stats{};
+	if (use_dilution && dilution == nullptr)
+	{
+		set_error("dilution table is required for dilution models.");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (prior == nullptr)
+	{
+		set_error("null prior pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	std::string why;
+	if (const int rc = check_supported(subjects, variants, &why))
+	{
+		set_error(why);
+		return rc;
+	}
+	const int resolved = selector == 0 ? (variants == 1 ? 1 : 2) : selector;
+	if (resolved != 1 && resolved != 2)
+	{
+		set_error("unsupported selector");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (resolved == 1 && variants != 1)
+	{
+		set_error("Op-BHA tree selection is only supported for binary lattices.");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (search_depth < 0 || search_depth > kMaxDepth)
+	{
+		set_error("search depth out of range");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (!bgt_cuda_provider_available())
+	{
+		set_error("no CUDA device");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	try
+	{
+		std::vector<double> flat;
+		if (use_dilution)
+		{
+			flat.assign(static_cast<size_t>(subjects) * (subjects + 1), 0.0);
+			for (int L = 1; L <= subjects; L++)
+				for (int c = 0; c <= L; c++)
+					flat[static_cast<size_t>(L - 1) * (subjects + 1) + c] = dilution[L - 1][c];
+		}
+		return run_tree(use_dilution, subjects, variants, prior, search_depth, threshold_up, threshold_lo,
+						branch_threshold, resolved, flat, stats);
+	}
+	catch (const std::exception &ex)
+	{
+		set_error(ex.what());
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+}
+
+int bgt_cuda_provider_benchmark_select(int subjects, int variants, const double *prior, int selector, int iterations,
+									   int warmup, uint32_t *candidate, double *init_seconds, double *mean_seconds,
+									   double *min_seconds, double *max_seconds, double *stddev_seconds)
+{
+	if (candidate == nullptr || init_seconds == nullptr || mean_seconds == nullptr || min_seconds == nullptr ||
+		max_seconds == nullptr || stddev_seconds == nullptr)
+	{
+		set_error("null output pointer");
+		return 1;
+	}
+	*candidate = 0;
+	*init_seconds = *mean_seconds = *min_seconds = *max_seconds = *stddev_seconds = 0.0;
+	if (iterations <= 0 || warmup < 0 || prior == nullptr)
+	{
+		set_error("invalid benchmark arguments");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	using Clock = std::chrono::steady_clock;
+	const auto t0 = Clock::now();
+	bgt_gpu_lattice *lat = nullptr;
+	int rc = bgt_gpu_lattice_create(0, subjects, variants, prior, BGT_GPU_FP64, &lat);
+	if (rc != 0)
+		return rc;
+	*init_seconds = std::chrono::duration<double>(Clock::now() - t0).count();
+	std::vector<double> times;
+	uint32_t e = 0;
+	for (int i = 0; i < warmup + iterations && rc == 0; i++)
+	{
+		const auto s = Clock::now();
+		rc = bgt_gpu_lattice_reselect(lat, selector, &e);
+		if (i >= warmup)
+			times.push_back(std::chrono::duration<double>(Clock::now() - s).count());
+	}
+	bgt_gpu_lattice_destroy(lat);
+	if (rc != 0)
+		return rc;
+	double sum = 0.0;
+	*min_seconds = std::numeric_limits<double>::max();
+	for (double t : times)
+	{
+		sum += t;
+		*min_seconds = std::min(*min_seconds, t);
+		*max_seconds = std::max(*max_seconds, t);
+	}
+	*mean_seconds = sum / static_cast<double>(times.size());
+	double var = 0.0;
+	for (double t : times)
+		var += (t - *mean_seconds) * (t - *mean_seconds);
+	*stddev_seconds = std::sqrt(var / static_cast<double>(times.size()));
+	*candidate = e;
+	return BGT_GPU_OK;
+}
+
+} // extern "C"

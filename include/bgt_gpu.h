@@ -1,0 +1,175 @@
+/*
+ * bgt_gpu.h -- C ABI of the GB300-native CUDA provider for the
+ * BayesianGroupTesting lattice hot path.
+ *
+ * The library (libbgt_gb300.so) owns all device memory.  Host pointers are
+ * borrowed for the duration of a call only.  No C++ exception crosses this
+ * boundary: every entry point returns an int status using the reference's
+ * CUDA-provider codes (src/kernels/cuda/cuda_provider.cu:2384-2445):
+ *
+ *   0  success
+ *   1  a dilution table (or another required pointer) is missing
+ *   2  unsupported request: limits, selector/variant combination, no device
+ *   3  (reserved by the reference for "MPI not initialised"; never returned)
+ *   4  runtime failure (CUDA error, zero normalising constant, ...)
+ *
+ * bgt_gpu_last_error() returns a thread-local description of the last
+ * failure.  Calls on one lattice or session handle are not thread-safe; each
+ * handle runs on its own CUDA stream.
+ *
+ * Bit conventions are the reference's internal ones: a state is a 32-bit word,
+ * atom index = variant * subjects + subject, bit set = negative (healthy);
+ * experiments are subject masks; response bit v set = pool tested negative for
+ * variant v.  Selector ids follow bgt::SelectorType (include/bgt/types.hpp:89-94):
+ * 0 = auto (Op-BHA for k = 1, Op-BBPA otherwise), 1 = Op-BHA, 2 = Op-BBPA.
+ * Lattice type ids: 0 = replicated non-dilution, 1 = replicated dilution.
+ */
+#ifndef BGT_GPU_H
+#define BGT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define BGT_GPU_API __declspec(dllexport)
+#else
+#define BGT_GPU_API __attribute__((visibility("default")))
+#endif
+
+/* Same layout as bgt::TreeStats (include/bgt/types.hpp:109-119). */
+typedef struct bgt_tree_stats
+{
+	int total_leaves;
+	double correct_probability;
+	double incorrect_probability;
+	double false_positive_probability;
+	double false_negative_probability;
+	double unclassified_probability;
+	double expected_stages;
+	double expected_tests;
+} bgt_tree_stats;
+
+enum bgt_gpu_status
+{
+	BGT_GPU_OK = 0,
+	BGT_GPU_MISSING_DILUTION = 1,
+	BGT_GPU_UNSUPPORTED = 2,
+	BGT_GPU_RUNTIME_FAILURE = 4
+};
+
+enum bgt_gpu_precision
+{
+	BGT_GPU_FP64 = 0,
+	/* FP32 posterior storage; fixed-point (exact integer) reductions and FP64
+	 * normalisation, thresholds and objective comparison. */
+	BGT_GPU_FP32 = 1
+};
+
+/* ------------------------------------------------------------------------
+ * Reference-compatible provider entry points.
+ * ------------------------------------------------------------------------ */
+
+/* Replaces int bgt_cuda_provider_available()
+ * (include/bgt/detail/cuda_provider.hpp:5): 1 when a CUDA device is usable. */
+BGT_GPU_API int bgt_cuda_provider_available(void);
+
+/* Replaces bgt_cuda_provider_run (include/bgt/detail/cuda_provider.hpp:6-9,
+ * src/kernels/cuda/cuda_provider.cu:2371-2445): builds the local adaptive
+ * testing tree to `search_depth` on the device and sweeps every true state,
+ * filling `stats`.  `dilution` is the reference DilutionTable row array
+ * (row L-1 holds L+1 entries) and is required when use_dilution != 0. */
+BGT_GPU_API int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const double *prior,
+									  int search_depth, double threshold_up, double threshold_lo,
+									  double branch_threshold, int selector, double **dilution,
+									  bgt_tree_stats *stats);
+
+/* Replaces bgt_cuda_provider_benchmark_select
+ * (include/bgt/detail/cuda_provider.hpp:14-24, cuda_provider.cu:2449-2551):
+ * builds the prior lattice, then times `iterations` selections after
+ * `warmup` untimed ones (host wall clock around a device synchronisation). */
+BGT_GPU_API int bgt_cuda_provider_benchmark_select(int subjects, int variants, const double *prior, int selector,
+												   int iterations, int warmup, uint32_t *candidate,
+												   double *init_seconds, double *mean_seconds, double *min_seconds,
+												   double *max_seconds, double *stddev_seconds);
+
+/* ------------------------------------------------------------------------
+ * Device lattice: the backing of a GPU bgt::Lattice::Impl
+ * (src/core/lattice_api.cpp:51-196 is the CPU counterpart).
+ * ------------------------------------------------------------------------ */
+
+typedef struct bgt_gpu_lattice bgt_gpu_lattice;
+
+/* bgt::Lattice(type, subjects, variants, prior) (include/bgt/lattice.hpp:228-229):
+ * allocates the 2^(subjects*variants) posterior and sets the product prior
+ * (src/core/model/lattice_base.cpp:184-208). */
+BGT_GPU_API int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const double *prior,
+									   int precision, bgt_gpu_lattice **out);
+BGT_GPU_API int bgt_gpu_lattice_destroy(bgt_gpu_lattice *lattice);
+
+/* Launch all of this lattice's work on `stream` (a cudaStream_t); 0 restores
+ * the lattice's own stream. */
+BGT_GPU_API int bgt_gpu_lattice_set_stream(bgt_gpu_lattice *lattice, void *stream);
+
+/* Lattice::select_experiment (include/bgt/lattice.hpp:244; CPU:
+ * src/kernels/cpu/bbpa.cpp:861-871).  Internal bit order. */
+BGT_GPU_API int bgt_gpu_lattice_select(bgt_gpu_lattice *lattice, int selector, uint32_t *experiment);
+
+/* Recomputes the selection from the posterior even when a cached result is
+ * current (one full zeta + argmin pass); used to time selection the way
+ * bgt_cuda_provider_benchmark_select does. */
+BGT_GPU_API int bgt_gpu_lattice_reselect(bgt_gpu_lattice *lattice, int selector, uint32_t *experiment);
+
+/* Lattice::update (include/bgt/lattice.hpp:246; CPU: lattice_api.cpp:170-174
+ * -> update_probs_in_place, lattice_base.cpp:230-244).  `dilution_rows` is
+ * the DilutionTable row array, required for dilution lattices. */
+BGT_GPU_API int bgt_gpu_lattice_update(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
+									   const double *const *dilution_rows);
+
+/* Lattice::update_classification (include/bgt/lattice.hpp:247; CPU:
+ * update_metadata, lattice_base.cpp:246-264).  Returns the accumulated masks. */
+BGT_GPU_API int bgt_gpu_lattice_classify(bgt_gpu_lattice *lattice, double threshold_up, double threshold_lo,
+										 uint32_t *positive_mask, uint32_t *negative_mask);
+
+/* Copies the normalised posterior (2^(subjects*variants) doubles) to `out`. */
+BGT_GPU_API int bgt_gpu_lattice_read_posterior(bgt_gpu_lattice *lattice, double *out);
+
+/* Lattice::posterior_probability / upset_probability_mass
+ * (include/bgt/lattice.hpp:241-242), internal bit order. */
+BGT_GPU_API int bgt_gpu_lattice_posterior_probability(bgt_gpu_lattice *lattice, uint32_t state, double *out);
+BGT_GPU_API int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, double *out);
+
+/* Per-atom posterior masses m_i (compute_atom_masses,
+ * lattice_base.cpp:25-41); `out` holds subjects*variants doubles. */
+BGT_GPU_API int bgt_gpu_lattice_atom_masses(bgt_gpu_lattice *lattice, double *out);
+
+/* ------------------------------------------------------------------------
+ * Device-driven adaptive sessions (no host round trip per stage).
+ * ------------------------------------------------------------------------ */
+
+/* Runs `stages` stages of select -> response -> update -> classify on the
+ * lattice, in the bgt::Lattice call order (lattice_api.cpp:108-178), with each
+ * response drawn on the device from the session's counter-based stream
+ * (include/bgt_session_rng.h) given `true_state`.  The lattice must hold the
+ * prior (freshly created).  Host outputs (each `stages` long, any may be
+ * null): selected experiments, responses, and the positive/negative masks
+ * after each stage.  Blocks until the session completes. */
+BGT_GPU_API int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, double alpha, double h,
+									double threshold_up, double threshold_lo, uint64_t seed, uint64_t session,
+									uint32_t true_state, uint32_t *experiments, uint32_t *responses,
+									uint32_t *positive_masks, uint32_t *negative_masks);
+
+/* Thread-local description of the last failure ("" when none). */
+BGT_GPU_API const char *bgt_gpu_last_error(void);
+
+/* Number of kernels this library has launched in this process (for launch
+ * accounting in benchmarks). */
+BGT_GPU_API uint64_t bgt_gpu_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

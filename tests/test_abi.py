@@ -1,0 +1,52 @@
+"""The C-ABI library builds, loads without a GPU and exports every entry
+point that include/*.h declares (no compute calls)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    for header in glob.glob(os.path.join(REPO, "include", "*.h")):
+        text = open(header).read()
+        names.update(re.findall(r"BGT_GPU_API\s+[\w\s\*]+?\b(\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_reference_entry_points():
+    names = _declared_symbols()
+    for ref in ("bgt_cuda_provider_available", "bgt_cuda_provider_run", "bgt_cuda_provider_benchmark_select"):
+        assert ref in names
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    missing = [n for n in _declared_symbols() if not hasattr(native_lib, n)]
+    assert not missing, missing
+
+
+def test_python_bindings_cover_the_header(native_lib):
+    from bayesiangrouptesting_gb300 import _native
+    assert set(_declared_symbols()) <= set(_native.SIGNATURES), set(_declared_symbols()) - set(_native.SIGNATURES)
+
+
+def test_tree_stats_layout_matches_reference():
+    from bayesiangrouptesting_gb300._native import TreeStatsC
+    # int total_leaves followed by seven doubles (include/bgt/types.hpp:109-119).
+    assert ctypes.sizeof(TreeStatsC) == 64
+    assert TreeStatsC.correct_probability.offset == 8
+
+
+def test_no_fallback_without_device(native_lib):
+    import bayesiangrouptesting_gb300 as bgt
+    if native_lib.bgt_cuda_provider_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(bgt.Error):
+        bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 3, [0.1, 0.2, 0.3])
+    cfg = bgt.SimulationConfig(subjects=2, prior=[0.2, 0.4], options=bgt.SimulationOptions(provider=bgt.Provider.cuda))
+    with pytest.raises(bgt.Error):
+        bgt.run_simulation(cfg)

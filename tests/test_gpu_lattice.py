@@ -1,0 +1,102 @@
+"""Parity of the device lattice (prior, update, selection, classification,
+sessions) against the CPU oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+import bayesiangrouptesting_gb300 as bgt
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12  # FP64 posterior tolerance (SURVEY 8d / reference tests/cpp/support/assertions.hpp:14-19)
+
+
+def _lattice(n, pi0, dilution=False):
+    t = bgt.LatticeType.replicated_dilution if dilution else bgt.LatticeType.replicated_non_dilution
+    return bgt.Lattice(t, n, pi0)
+
+
+def _near_tie_ok(oracle, post, n, chosen, expected):
+    """A selection mismatch is accepted only at a documented near-tie: the
+    oracle's own Op-BHA distances of both experiments differ by <= 1e-12."""
+    if chosen == expected:
+        return True
+    _, upset = oracle.op_bha(post, n)
+    a, b = abs(upset[chosen] - 0.5), abs(upset[expected] - 0.5)
+    return abs(a - b) <= 1e-12 * max(1.0, a)
+
+
+def test_prior_matches_oracle(gpu, oracle):
+    rng = np.random.default_rng(1)
+    for n in (1, 2, 5, 13, 14, 15, 18, 20):
+        pi0 = rng.uniform(0.01, 0.3, n)
+        lat = _lattice(n, pi0)
+        got = lat.posterior()
+        want = oracle.prior(pi0)
+        np.testing.assert_allclose(got, want, rtol=RTOL, atol=0)
+
+
+def test_reference_pins_public_order(gpu):
+    # tests/cpp/unit/lattice_api_test.cpp:63-91 (public, bit-reversed order).
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 2, [0.2, 0.4])
+    for s, v in enumerate([0.08, 0.12, 0.32, 0.48]):
+        assert abs(lat.posterior_probability(s) - v) <= 1e-12
+    for e, v in ((1, 0.60), (2, 0.80), (3, 0.48)):
+        assert abs(lat.upset_probability_mass(e) - v) <= 1e-12
+    for sel in (bgt.SelectorType.auto_select, bgt.SelectorType.op_bha, bgt.SelectorType.op_bbpa):
+        assert lat.select_experiment(sel) == 3
+    lat.update(1, 1)
+    den = 0.60 * 0.99 + 0.40 * 0.01
+    for s, v in enumerate([0.08 * 0.01 / den, 0.12 * 0.99 / den, 0.32 * 0.01 / den, 0.48 * 0.99 / den]):
+        assert abs(lat.posterior_probability(s) - v) <= 1e-12
+    lat.update_classification(0.01, 0.01)
+    assert lat.positive_classification_mask() == 0
+    assert lat.negative_classification_mask() == 1
+    assert not lat.is_classified()
+
+
+@pytest.mark.parametrize("dilution", [False, True])
+def test_update_and_select_sequence(gpu, oracle, dilution):
+    rng = np.random.default_rng(2 + dilution)
+    for n in (3, 9, 14, 16, 19):
+        pi0 = rng.uniform(0.01, 0.25, n)
+        lat = _lattice(n, pi0, dilution)
+        post = oracle.prior(pi0)
+        table = bgt.api.DilutionTable(n, 0.99, 0.005) if dilution else None
+        for step in range(4):
+            e_int = oracle.select(post, n, 1, 1)
+            got_int = bgt.reverse_bits(lat.select_experiment(bgt.SelectorType.op_bha), n)
+            assert _near_tie_ok(oracle, post, n, got_int, e_int), (n, step, got_int, e_int)
+            e = e_int if e_int != 0 else 1
+            r = int(rng.integers(0, 2))
+            post = oracle.update(1 if dilution else 0, n, 1, post, e, r, 0.99, 0.005, in_place=True)
+            lat.update(bgt.reverse_bits(e, n), r, table)
+            np.testing.assert_allclose(lat.posterior(), post, rtol=RTOL, atol=1e-300)
+            masses = oracle.atom_masses(post, n)
+            np.testing.assert_allclose(lat.atom_masses(), masses, rtol=1e-12, atol=1e-18)
+
+
+@pytest.mark.parametrize("dilution,alpha", [(False, 0.99), (True, 0.99), (True, 0.01)])
+def test_device_session_matches_oracle(gpu, oracle, dilution, alpha):
+    rng = np.random.default_rng(11)
+    for n in (4, 10, 15, 18):
+        pi0 = rng.uniform(0.005, 0.10, n)
+        truth = int(rng.integers(0, 1 << n)) | int(rng.integers(0, 1 << n))
+        for selector in (1, 2):
+            lat = _lattice(n, pi0, dilution)
+            got = lat.run_session(8, truth, seed=5, session=3, selector=selector, alpha=alpha)
+            want = oracle.session(1 if dilution else 0, n, 1, pi0, 8, 5, 3, truth, selector=selector, alpha=alpha)
+            np.testing.assert_array_equal(got["experiments"], want["experiments"])
+            np.testing.assert_array_equal(got["responses"], want["responses"])
+            np.testing.assert_array_equal(got["pos"], want["pos"])
+            np.testing.assert_array_equal(got["neg"], want["neg"])
+            np.testing.assert_allclose(lat.posterior(), want["posterior"], rtol=RTOL, atol=1e-300)
+
+
+def test_errors_are_loud(gpu):
+    with pytest.raises(ValueError):
+        bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 3, [0.1, 0.2])
+    lat = _lattice(3, [0.1, 0.2, 0.3], dilution=True)
+    with pytest.raises(ValueError):
+        lat.update(1, 1, None)
+    with pytest.raises(bgt.Error):
+        bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 31, [0.1] * 31)

@@ -1,0 +1,59 @@
+"""Tree simulation parity (bgt_cuda_provider_run through run_simulation)
+against the CPU oracle: the reference's CUDA parity cases
+(tests/cpp/integration/cuda_tree_parity_test.cpp:75-150), the single-subject
+golden (tests/cpp/support/assertions.hpp:80-92) and BASELINE-sized trees."""
+import numpy as np
+import pytest
+
+import bayesiangrouptesting_gb300 as bgt
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _run(dilution, n, pi0, depth, up=0.01, lo=0.01, branch=0.0, selector=0, alpha=0.99, h=0.005):
+    cfg = bgt.SimulationConfig(
+        lattice_type=bgt.LatticeType.replicated_dilution if dilution else bgt.LatticeType.replicated_non_dilution,
+        subjects=n, variants=1, prior=list(pi0),
+        options=bgt.SimulationOptions(search_depth=depth, threshold_up=up, threshold_lo=lo, branch_threshold=branch,
+                                      selector=bgt.SelectorType(selector), provider=bgt.Provider.cuda),
+        dilution=bgt.api.DilutionParameters(alpha, h))
+    return bgt.run_simulation(cfg).stats.as_array()
+
+
+def _check(got, want):
+    assert got[0] == want[0], (got, want)
+    np.testing.assert_allclose(got[1:], want[1:], rtol=TOL, atol=TOL)
+
+
+def test_single_subject_golden(gpu):
+    got = _run(False, 1, [0.2], 1)
+    _check(got, np.array([2, 0.792, 0.002, 0.0, 0.002, 0.206, 1.0, 1.0]))
+
+
+@pytest.mark.parametrize("case", [
+    (False, 2, [0.2, 0.4], 1, 0.0, 0),
+    (True, 2, [0.2, 0.4], 1, 0.0, 0),
+    (False, 3, [0.02, 0.05, 0.1], 3, 0.001, 1),
+    (False, 3, [0.02, 0.05, 0.1], 3, 0.001, 2),
+    (True, 3, [0.02, 0.05, 0.1], 3, 0.001, 1),
+    (True, 3, [0.02, 0.05, 0.1], 3, 0.001, 2),
+    (False, 2, [0.2, 0.7], 2, 0.0, 0),
+    (True, 2, [0.2, 0.7], 2, 0.0, 0),
+])
+def test_reference_parity_cases(gpu, oracle, case):
+    dil, n, pi0, depth, branch, sel = case
+    up = lo = 0.1 if pi0 == [0.2, 0.7] else 0.01
+    got = _run(dil, n, pi0, depth, up, lo, branch, sel)
+    want = oracle.run_simulation(1 if dil else 0, n, 1, pi0, depth, up, lo, branch, sel)
+    _check(got, want)
+
+
+@pytest.mark.parametrize("n,depth,dil", [(8, 5, False), (10, 6, True), (12, 4, False), (16, 4, False)])
+def test_seeded_trees(gpu, oracle, n, depth, dil):
+    rng = np.random.default_rng(100 + n)
+    pi0 = rng.uniform(0.01, 0.20, n)
+    got = _run(dil, n, pi0, depth)
+    want = oracle.run_simulation(1 if dil else 0, n, 1, pi0, depth)
+    _check(got, want)
