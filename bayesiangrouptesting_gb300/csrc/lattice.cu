@@ -3,6 +3,7 @@
 // include/bgt_gpu.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -22,8 +23,8 @@
 namespace bgt_gpu
 {
 
-__global__ void k1_zeta_low(LatticeDev *states);
-__global__ void k2_zeta_high_select(LatticeDev *states);
+__global__ void k1_zeta_low(LatticeDev *states, int count, int per);
+__global__ void k2_zeta_high_select(LatticeDev *states, int count, int per);
 __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
 __global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, unsigned long long *out);
 
@@ -42,8 +43,20 @@ void cuda_check(cudaError_t err, const char *what)
 		throw CudaFailure(std::string(what) + ": " + cudaGetErrorString(err));
 }
 
-size_t k1_smem_bytes() { return sizeof(unsigned long long) << kTileBits; }
-size_t k2_smem_bytes(int hbits) { return (sizeof(unsigned long long) * kColW + sizeof(int)) << hbits; }
+size_t k1_smem_bytes() { return kPipeSmem; }
+size_t k2_smem_bytes(int) { return kPipeSmem; }
+
+int sm_count()
+{
+	static int sms = 0;
+	if (sms == 0)
+	{
+		cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0), "sm count");
+		if (sms <= 0)
+			sms = 1;
+	}
+	return sms;
+}
 
 void configure_kernels()
 {
@@ -54,23 +67,25 @@ void configure_kernels()
 									static_cast<int>(k1_smem_bytes())),
 			   "k1 smem attribute");
 	cuda_check(cudaFuncSetAttribute(k2_zeta_high_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
-									static_cast<int>(k2_smem_bytes(kMaxHighBits))),
+									static_cast<int>(k2_smem_bytes(0))),
 			   "k2 smem attribute");
 	done = true;
 }
 
 void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream)
 {
-	dim3 grid(1u << g.hbits, static_cast<unsigned>(count));
-	k1_zeta_low<<<grid, kTileThreads, k1_smem_bytes(), stream>>>(states);
+	const long long items = static_cast<long long>(count) << g.hbits;
+	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, count, 1 << g.hbits);
 	cuda_check(cudaGetLastError(), "k1 launch");
 	count_launches(1);
 }
 
 void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream)
 {
-	dim3 grid(static_cast<unsigned>(g.nblk), static_cast<unsigned>(count));
-	k2_zeta_high_select<<<grid, kHighThreads, k2_smem_bytes(g.hbits), stream>>>(states);
+	const long long items = static_cast<long long>(count) * g.nblk;
+	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, count, g.nblk);
 	cuda_check(cudaGetLastError(), "k2 launch");
 	count_launches(1);
 }
@@ -83,7 +98,15 @@ LatticeGeometry make_geometry(int n, int k)
 	g.atoms = n * k;
 	g.tbits = g.atoms < kTileBits ? g.atoms : kTileBits;
 	g.hbits = g.atoms - g.tbits;
-	g.nblk = (1 << g.tbits) >= kColW ? (1 << g.tbits) / kColW : 1;
+	int w = kTileElems >> g.hbits;
+	w = std::max(w, kMinColW);
+	w = std::min(w, kMaxColW);
+	w = std::min(w, 1 << g.tbits);
+	g.colw = w;
+	g.logw = 0;
+	while ((1 << g.logw) < w)
+		g.logw++;
+	g.nblk = (1 << g.tbits) / w;
 	return g;
 }
 
@@ -200,6 +223,8 @@ struct bgt_gpu_lattice
 			throw CudaFailure("posterior normalising constant is zero");
 		if (err == kErrNonFinite)
 			throw CudaFailure("non-finite posterior value");
+		if (err == kErrTimeout)
+			throw CudaFailure("a bulk copy did not complete in time");
 	}
 
 	void run_k1()
@@ -318,7 +343,7 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			const size_t rows = size_t{1} << g.hbits;
 			cuda_check(cudaMalloc(&lat->dev, sizeof(LatticeDev)), "alloc state");
 			cuda_check(cudaMalloc(&lat->q, states * sizeof(double)), "alloc posterior");
-			cuda_check(cudaMalloc(&lat->m1, static_cast<size_t>(g.nblk) * rows * kColW * sizeof(unsigned long long)),
+			cuda_check(cudaMalloc(&lat->m1, static_cast<size_t>(g.nblk) * rows * g.colw * sizeof(unsigned long long)),
 					   "alloc zeta partials");
 			cuda_check(cudaMalloc(&lat->tile_total, rows * sizeof(unsigned long long)), "alloc tile totals");
 			cuda_check(cudaMalloc(&lat->tile_scale, rows * sizeof(int)), "alloc tile scales");
@@ -345,6 +370,9 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			h.tbits = g.tbits;
 			h.hbits = g.hbits;
 			h.nblk = g.nblk;
+			h.colw = g.colw;
+			h.logw = g.logw;
+			h.masses_in_k2 = 1;
 			h.dilution = lattice_type;
 			h.orig_n = subjects;
 			h.q_in = lat->q;
@@ -671,17 +699,17 @@ int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, doub
 				   "session setup");
 		lattice->set_field(offsetof(LatticeDev, pos), lattice->pos);
 		lattice->set_field(offsetof(LatticeDev, neg), lattice->neg);
-		lattice->set_field(offsetof(LatticeDev, classify_on_update), 1);
-		// Stage loop: K2 selects and queues the update, K1 applies it and classifies.
+		// Stage loop: K2 selects (and classifies the previous update's
+		// posterior) and queues the update, K1 applies it.
+		launch_k2(lattice->dev, 1, lattice->g, lattice->stream);
 		for (int s = 0; s < stages; s++)
 		{
-			launch_k2(lattice->dev, 1, lattice->g, lattice->stream);
 			launch_k1(lattice->dev, 1, lattice->g, lattice->stream);
+			launch_k2(lattice->dev, 1, lattice->g, lattice->stream);
 		}
-		lattice->set_field(offsetof(LatticeDev, classify_on_update), 0);
 		lattice->k1_pending = false;
 		lattice->update_pending = false;
-		lattice->k2_valid = false;
+		lattice->k2_valid = true;
 		std::vector<unsigned int> host(4 * S);
 		cuda_check(cudaMemcpyAsync(host.data(), o, host.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost,
 								   lattice->stream),

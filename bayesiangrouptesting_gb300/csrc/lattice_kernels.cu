@@ -1,17 +1,23 @@
 // Kernels of the GB300 lattice provider (see lattice_kernels.cuh for the
-// design).  All kernels index the lattice they work on through
-// states[blockIdx.y], so one launch can sweep many same-shape lattices (all
-// tree nodes of one depth, or a batch of sessions).
+// design).  K1 and K2 are persistent: each CTA walks a strided list of work
+// items (lattice, tile) drawn from a batch of same-shape lattices, with the
+// next item's 64 KB tile already in flight on the TMA engine (cp.async.bulk
+// into a second shared-memory buffer, completion on an mbarrier) while the
+// current tile is transformed.  A lattice's epilogue runs in whichever CTA
+// completes its last work item.
 #include <cuda_runtime.h>
 
 #include "lattice_kernels.cuh"
+#include "pipeline.cuh"
 
 namespace bgt_gpu
 {
 
-// ------------------------------------------------------------------ K1
+typedef unsigned long long u64;
 
-// Classification of one atom from its fixed-point mass (update_metadata,
+// ------------------------------------------------------------ shared pieces
+
+// Classification of the atoms from their fixed-point masses (update_metadata,
 // src/core/model/lattice_base.cpp:246-264): mass < lo -> positive,
 // mass > 1 - up -> negative, classified atoms are never revisited.
 __device__ __forceinline__ void classify_atoms(LatticeDev &L, double up, double lo)
@@ -33,263 +39,243 @@ __device__ __forceinline__ void classify_atoms(LatticeDev &L, double up, double 
 	L.neg = neg;
 }
 
+// Index of the j-th value of thread t in each phase of the 13-bit in-tile
+// zeta (512 threads x 16 values).  The four bits of j are the tile bits
+// {0,10,11,12} (A), 6..9 (B), 2..5 (C) and 0..3 (D); the other nine bits
+// come from t.  A keeps adjacent pairs (bit 0) in one thread so that the
+// input and q' move as 16-byte accesses; D gives each thread 16 consecutive
+// columns.  With the tile_swz layout every phase is free of shared-memory
+// bank conflicts for 8-byte accesses.
+__device__ __forceinline__ unsigned int map_a(unsigned int t, int j)
+{
+	return (static_cast<unsigned int>(j) & 1u) | (t << 1) | ((static_cast<unsigned int>(j) >> 1) << 10);
+}
+__device__ __forceinline__ unsigned int map_b(unsigned int t, int j)
+{
+	return (t & 63u) | (static_cast<unsigned int>(j) << 6) | ((t >> 6) << 10);
+}
+__device__ __forceinline__ unsigned int map_c(unsigned int t, int j)
+{
+	return (t & 3u) | (static_cast<unsigned int>(j) << 2) | ((t >> 2) << 6);
+}
+__device__ __forceinline__ unsigned int map_d(unsigned int t, int j) { return static_cast<unsigned int>(j) | (t << 4); }
 
-// Block-wide float sum over 1024 threads; result valid in every thread.
-__device__ __forceinline__ float block_sum_1024(float v, float *red)
+// Zeta butterfly over register bit `lvl` when tile bit `bit` is in `mask`.
+__device__ __forceinline__ void reg_level(u64 (&a)[kPerThread], int lvl, int bit, unsigned int mask)
+{
+	if (mask & (1u << bit))
+	{
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			if (!(j & (1 << lvl)))
+				a[j] += a[j | (1 << lvl)];
+	}
+}
+
+// The register bits of each phase, in order: A = {0, 10, 11, 12},
+// B = {6, 7, 8, 9}, C = {2, 3, 4, 5}, D = {0, 1, 2, 3} (only bit 1 remains).
+__device__ __forceinline__ void levels_a(u64 (&a)[kPerThread], unsigned int mask)
+{
+	reg_level(a, 0, 0, mask);
+	reg_level(a, 1, 10, mask);
+	reg_level(a, 2, 11, mask);
+	reg_level(a, 3, 12, mask);
+}
+__device__ __forceinline__ void levels_b(u64 (&a)[kPerThread], unsigned int mask)
+{
+#pragma unroll
+	for (int l = 0; l < 4; l++)
+		reg_level(a, l, 6 + l, mask);
+}
+__device__ __forceinline__ void levels_c(u64 (&a)[kPerThread], unsigned int mask)
+{
+#pragma unroll
+	for (int l = 0; l < 4; l++)
+		reg_level(a, l, 2 + l, mask);
+}
+
+// Block-wide float sum over 512 threads; valid in every thread.  The barrier
+// also votes: `abort` becomes true in every thread if any thread passed true.
+__device__ __forceinline__ float block_sum(float v, float *red, bool &abort)
 {
 	for (int o = 16; o > 0; o >>= 1)
 		v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	if (lane == 0)
-		red[warp] = v;
-	__syncthreads();
-	float t = lane < (kTileThreads / 32) ? red[lane] : 0.0f;
+	if ((threadIdx.x & 31) == 0)
+		red[threadIdx.x >> 5] = v;
+	abort = __syncthreads_or(abort) != 0;
+	float t = (threadIdx.x & 31) < (kThreads / 32) ? red[threadIdx.x & 31] : 0.0f;
 	for (int o = 16; o > 0; o >>= 1)
 		t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
 	return t;
 }
 
-// In-register zeta over the 4 bits of the per-thread index i, for those of
-// the lattice bits `bit0 .. bit0+3` that lie below `tbits`.
-__device__ __forceinline__ void reg_zeta16(unsigned long long (&a)[kPerThread], int bit0, int tbits)
+__device__ __forceinline__ void argmin_warp(u64 &s, unsigned int &e)
 {
-#pragma unroll
-	for (int lvl = 0; lvl < 4; lvl++)
+	for (int o = 16; o > 0; o >>= 1)
 	{
-		if (bit0 + lvl < tbits)
+		const u64 os = __shfl_xor_sync(0xFFFFFFFFu, s, o);
+		const unsigned int oe = __shfl_xor_sync(0xFFFFFFFFu, e, o);
+		if (better(os, oe, s, e))
 		{
-#pragma unroll
-			for (int i = 0; i < kPerThread; i++)
-				if (!(i & (1 << lvl)))
-					a[i] += a[i | (1 << lvl)];
+			s = os;
+			e = oe;
 		}
 	}
 }
 
-// One K1 tile: see the header.  Dynamic shared memory: 2^14 u64.
-__global__ void __launch_bounds__(kTileThreads, 1) k1_zeta_low(LatticeDev *states)
+// Block argmin (lowest index on ties); result valid in thread 0.
+__device__ __forceinline__ void argmin_block(u64 &s, unsigned int &e, u64 *ws, unsigned int *we)
 {
-	extern __shared__ unsigned long long sm[];
-	__shared__ double ctab[kMaxClasses];
-	__shared__ float red[32];
-	__shared__ int s_flag;
-	LatticeDev &L = states[blockIdx.y];
+	argmin_warp(s, e);
+	if ((threadIdx.x & 31) == 0)
+	{
+		ws[threadIdx.x >> 5] = s;
+		we[threadIdx.x >> 5] = e;
+	}
+	__syncthreads();
+	if (threadIdx.x < 32)
+	{
+		s = threadIdx.x < kThreads / 32 ? ws[threadIdx.x] : ~0ull;
+		e = threadIdx.x < kThreads / 32 ? we[threadIdx.x] : 0xFFFFFFFFu;
+		argmin_warp(s, e);
+	}
+}
+
+// Per-lattice constants of the lattice a CTA is currently working on, read
+// once from global memory when the lattice changes.
+struct LatCache
+{
+	int li;
+	int mode, tbits, hbits, colw, logw, dilution, skip, n;
+	unsigned int e, active;
+	const double *q_in;
+	double *q_out;
+	u64 *m1;
+	const double *prior_lo;
+	const double *prior_hi;
+	double c_in, c_out;
+	u64 zg;
+	int masses;
+	u64 *tile_total;
+	int *tile_scale;
+};
+
+struct PipeShared
+{
+	uint64_t bars[2];
+	LatCache lc;
+	double ctab[kMaxClasses];
+	float fred[32];
+	u64 ws[32];
+	unsigned int we[32];
+	double dred[32];
+	u64 ured[32];
+	int flag;
+	int last;
+	int abort;
+	int cached_lattice;
+};
+
+// Shared memory of the persistent passes, as file-scope symbols so that every
+// access compiles to a shared-memory instruction: two 64 KB bulk-copy tile
+// buffers and one 64 KB work tile (dynamic), the pipeline state, and K2's
+// per-row rescale shifts.
+extern __shared__ __align__(1024) unsigned char g_smem[];
+__shared__ PipeShared ps;
+__shared__ int g_shift[1 << kMaxHighBits];
+
+__device__ __forceinline__ double *tile_f64(int b) { return reinterpret_cast<double *>(g_smem + b * kSmemBuf); }
+__device__ __forceinline__ u64 *tile_u64(int b) { return reinterpret_cast<u64 *>(g_smem + b * kSmemBuf); }
+__device__ __forceinline__ u64 *work_tile() { return reinterpret_cast<u64 *>(g_smem + 2 * kSmemBuf); }
+
+// ------------------------------------------------------------------ K1
+
+// K1 epilogue of lattice L (whole CTA): global scale, exact total, and in
+// tree mode the exact atom marginals and the classification.
+__device__ void k1_epilogue(LatticeDev &L, int mode)
+{
 	const int tid = threadIdx.x;
 	const int tbits = L.tbits;
-	const int hbits = L.hbits;
-	const unsigned int tsize = 1u << tbits;
-	const unsigned int row = blockIdx.x;
-	const unsigned long long base = static_cast<unsigned long long>(row) << tbits;
-	const int mode = L.mode;
-	const unsigned int e = L.pend_e;
-
-	if (tid == 0)
-		s_flag = 0;
-	if (mode == kUpdate && tid < kMaxClasses)
-	{
-		const int pool = __popc(e);
-		double c = 0.0;
-		if (tid <= pool)
-			c = binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1) / L.z_norm;
-		ctab[tid] = c;
-	}
-	__syncthreads();
-
-	// Phase A: x = tid + 1024 i (lattice bits 10..13 in registers).
-	double v[kPerThread];
-	float f = 0.0f;
-	int bad = 0;
-	const double *q_in = L.q_in;
-	double *q_out = L.q_out;
-#pragma unroll
-	for (int i = 0; i < kPerThread; i++)
-	{
-		const unsigned int x = static_cast<unsigned int>(tid) + static_cast<unsigned int>(kTileThreads) * i;
-		double val = 0.0;
-		if (x < tsize)
-		{
-			const unsigned long long s = base | x;
-			if (mode == kGenerate)
-				val = L.prior_hi[row] * L.prior_lo[x];
-			else
-				val = q_in[s];
-			if (mode == kUpdate)
-				val *= ctab[__popc(e & static_cast<unsigned int>(s))];
-			if (mode != kLoad)
-				q_out[s] = val;
-		}
-		bad |= ((static_cast<unsigned long long>(__double_as_longlong(val)) >> 52) & 0x7FF) == 0x7FF;
-		v[i] = val;
-		f += approx_scaled(val);
-	}
-	if (bad)
-		s_flag = 1;
-	const float tile_est = block_sum_1024(f, red);
-	// Scale so that the tile total lands in [2^61, 2^62 * (1 + 2^-22)).
-	const int ef = (__float_as_int(tile_est) >> 23) & 0xFF;
-	const int scale = ef == 0 ? 237 : 252 - ef;
-
-	unsigned long long a[kPerThread];
-#pragma unroll
-	for (int i = 0; i < kPerThread; i++)
-		a[i] = to_fixed(v[i], scale);
-	reg_zeta16(a, 10, tbits);
-#pragma unroll
-	for (int i = 0; i < kPerThread; i++)
-		sm[tile_swz(static_cast<unsigned int>(tid) + kTileThreads * i)] = a[i];
-	__syncthreads();
-
-	// Phase B: lattice bits 6..9 in registers.
-	{
-		const unsigned int xb = (tid & 63) | ((tid >> 6) << 10);
-#pragma unroll
-		for (int i = 0; i < kPerThread; i++)
-			a[i] = sm[tile_swz(xb | (i << 6))];
-		reg_zeta16(a, 6, tbits);
-#pragma unroll
-		for (int i = 0; i < kPerThread; i++)
-			sm[tile_swz(xb | (i << 6))] = a[i];
-	}
-	__syncthreads();
-	// Phase C: lattice bits 2..5 in registers.
-	{
-		const unsigned int xc = (tid & 3) | ((tid >> 2) << 6);
-#pragma unroll
-		for (int i = 0; i < kPerThread; i++)
-			a[i] = sm[tile_swz(xc | (i << 2))];
-		reg_zeta16(a, 2, tbits);
-#pragma unroll
-		for (int i = 0; i < kPerThread; i++)
-			sm[tile_swz(xc | (i << 2))] = a[i];
-	}
-	__syncthreads();
-	// Phase D: lattice bits 0..1 in registers; thread tid owns column block tid.
-	{
-		const unsigned int xd = static_cast<unsigned int>(tid) << 4;
-#pragma unroll
-		for (int i = 0; i < kPerThread; i++)
-			a[i] = sm[tile_swz(xd | i)];
-#pragma unroll
-		for (int lvl = 0; lvl < 2; lvl++)
-		{
-			if (lvl < tbits)
-			{
-#pragma unroll
-				for (int i = 0; i < kPerThread; i++)
-					if (!(i & (1 << lvl)))
-						a[i] += a[i | (1 << lvl)];
-			}
-		}
-		if (xd < tsize || tid == 0)
-		{
-			const unsigned int rows = 1u << hbits;
-			unsigned long long *dst = L.m1 + (static_cast<size_t>(tid) * rows + row) * kColW;
-#pragma unroll
-			for (int i = 0; i < kPerThread; i += 2)
-				*reinterpret_cast<ulonglong2 *>(dst + i) = make_ulonglong2(a[i], a[i + 1]);
-		}
-		if (tid == 0)
-		{
-			L.tile_total[row] = a[0];
-			L.tile_scale[row] = scale;
-		}
-	}
-
-	// Last CTA of this lattice: global scale and exact total.
-	__shared__ bool s_last;
-	__syncthreads();
-	if (tid == 0)
-	{
-		if (s_flag)
-			atomicExch(&L.error, kErrNonFinite);
-		__threadfence();
-		const unsigned int prev = atomicAdd(&L.k1_count, 1u);
-		s_last = prev == gridDim.x - 1;
-	}
-	__syncthreads();
-	if (!s_last)
-		return;
-	__threadfence();
-	const unsigned int rows = 1u << hbits;
-	__shared__ double dred[32];
-	__shared__ unsigned long long ured[32];
+	const unsigned int rows = 1u << L.hbits;
 	double zr = 0.0;
-	for (unsigned int rr = tid; rr < rows; rr += kTileThreads)
-	{
-		const unsigned long long t = __ldcg(L.tile_total + rr);
-		const int sc = __ldcg(L.tile_scale + rr);
-		zr += __ull2double_rn(t) * pow2_neg(sc);
-	}
+	for (unsigned int rr = tid; rr < rows; rr += kThreads)
+		zr += __ull2double_rn(__ldcg(L.tile_total + rr)) * pow2_neg(__ldcg(L.tile_scale + rr));
 	for (int o = 16; o > 0; o >>= 1)
 		zr += __shfl_xor_sync(0xFFFFFFFFu, zr, o);
 	if ((tid & 31) == 0)
-		dred[tid >> 5] = zr;
+		ps.dred[tid >> 5] = zr;
 	__syncthreads();
 	if (tid < 32)
 	{
-		double t = dred[tid];
+		double t = tid < kThreads / 32 ? ps.dred[tid] : 0.0;
 		for (int o = 16; o > 0; o >>= 1)
 			t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
 		if (tid == 0)
-			dred[0] = t;
+			ps.dred[0] = t;
 	}
 	__syncthreads();
-	const double z_real = dred[0];
-	const int ez = static_cast<int>((static_cast<unsigned long long>(__double_as_longlong(z_real)) >> 52) & 0x7FF);
-	const int s_g = 1084 - ez;
-	unsigned long long zg = 0;
-	for (unsigned int rr = tid; rr < rows; rr += kTileThreads)
-		zg += rescale(__ldcg(L.tile_total + rr), s_g - __ldcg(L.tile_scale + rr));
+	const double z_real = ps.dred[0];
+	const int ez = static_cast<int>((static_cast<u64>(__double_as_longlong(z_real)) >> 52) & 0x7FF);
+	// Global scale: the total lands below 2^62 and no tile is ever scaled up
+	// (so K2 only shifts right).
+	int smin = 1 << 20;
+	for (unsigned int rr = tid; rr < rows; rr += kThreads)
+		smin = min(smin, __ldcg(L.tile_scale + rr));
+	for (int o = 16; o > 0; o >>= 1)
+		smin = min(smin, __shfl_xor_sync(0xFFFFFFFFu, smin, o));
+	if ((tid & 31) == 0)
+		ps.we[tid >> 5] = static_cast<unsigned int>(smin);
+	__syncthreads();
+	for (int ww = 0; ww < kThreads / 32; ww++)
+		smin = min(smin, static_cast<int>(ps.we[ww]));
+	const int s_g = min(1084 - ez, smin);
+	u64 zg = 0;
+	for (unsigned int rr = tid; rr < rows; rr += kThreads)
+		zg += shr_round(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
 	for (int o = 16; o > 0; o >>= 1)
 		zg += __shfl_xor_sync(0xFFFFFFFFu, zg, o);
 	__syncthreads();
 	if ((tid & 31) == 0)
-		ured[tid >> 5] = zg;
+		ps.ured[tid >> 5] = zg;
 	__syncthreads();
-	__shared__ unsigned long long s_zg;
-	if (tid < 32)
+	const bool tree_masses = mode == kUpdate && L.classify_on_update;
+	if (tree_masses)
 	{
-		unsigned long long t = ured[tid];
-		for (int o = 16; o > 0; o >>= 1)
-			t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
-		if (tid == 0)
-			s_zg = t;
-	}
-	__syncthreads();
-	// Exact atom marginals at the global scale: warp w sums atom w over the
-	// tiles.  Low atoms read the singleton column 1 << w of every tile's
-	// partial sums; high atoms add the totals of the tiles whose row index has
-	// bit w - tbits set.
-	{
+		// Warp w sums atom w over the tiles: low atoms from the singleton
+		// column 1 << w of every tile, high atoms from the tile totals.
 		const int warp = tid >> 5, lane = tid & 31;
-		if (warp < L.atoms)
+		const int logw = L.logw;
+		for (int atom = warp; atom < L.atoms; atom += kThreads / 32)
 		{
-			unsigned long long acc = 0;
-			if (warp < tbits)
+			u64 acc = 0;
+			if (atom < tbits)
 			{
-				const unsigned int col = 1u << warp;
-				const unsigned long long *src = L.m1 + (static_cast<size_t>(col / kColW) * rows) * kColW + (col % kColW);
+				const unsigned int col = 1u << atom;
+				const u64 *src = L.m1 + (static_cast<size_t>(col >> logw) * rows) * L.colw + (col & (L.colw - 1));
 				for (unsigned int rr = lane; rr < rows; rr += 32)
-					acc += rescale(__ldcg(src + static_cast<size_t>(rr) * kColW), s_g - __ldcg(L.tile_scale + rr));
+					acc += shr_round(__ldcg(src + static_cast<size_t>(rr) * L.colw),
+									 min(__ldcg(L.tile_scale + rr) - s_g, 63));
 			}
 			else
 			{
-				const unsigned int hb = 1u << (warp - tbits);
+				const unsigned int hb = 1u << (atom - tbits);
 				for (unsigned int rr = lane; rr < rows; rr += 32)
 					if (rr & hb)
-						acc += rescale(__ldcg(L.tile_total + rr), s_g - __ldcg(L.tile_scale + rr));
+						acc += shr_round(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
 			}
 			for (int o = 16; o > 0; o >>= 1)
 				acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
 			if (lane == 0)
-				L.atom_fixed[warp] = acc;
+				L.atom_fixed[atom] = acc;
 		}
 	}
 	__syncthreads();
 	if (tid == 0)
 	{
+		u64 t = 0;
+		for (int w = 0; w < kThreads / 32; w++)
+			t += ps.ured[w];
 		__threadfence();
-		const unsigned long long t = s_zg;
 		L.s_g = s_g;
 		L.z_g = t;
 		if (t == 0 || ez == 0)
@@ -301,163 +287,387 @@ __global__ void __launch_bounds__(kTileThreads, 1) k1_zeta_low(LatticeDev *state
 		if (mode != kLoad)
 			L.q_in = L.q_out;
 		L.mode = kLoad;
-		if (mode == kUpdate && L.classify_on_update)
-		{
+		if (tree_masses)
 			classify_atoms(L, L.up, L.lo);
-			if (L.sess_active)
+		L.k1_count = 0;
+	}
+	__syncthreads();
+}
+
+// The per-lattice values a work item needs, read once into registers (the
+// lattice state lives in global memory and would otherwise be re-read after
+// every barrier).
+struct ItemCfg
+{
+	double *q_out;
+	u64 *m1;
+	const double *prior_lo;
+	double phi;
+	unsigned int e;
+	int tbits, hbits, colw, logw;
+	int dilution_classes; // 1: class = popcount(e & s); 0: class = contained
+	double c_in, c_out;   // non-dilution update factors (contained / not)
+};
+
+// One K1 work item (tile r of lattice L), specialised on the K1 mode.
+template <int kMode>
+__device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int b, bool abort, u64 &total_out,
+										int &scale_out)
+{
+	double *const in = tile_f64(b);
+	u64 *const work = work_tile();
+	const unsigned int tid = threadIdx.x;
+	const int tbits = cfg.tbits;
+	const unsigned int tsize = 1u << tbits;
+	const unsigned int e = cfg.e;
+	const size_t base = static_cast<size_t>(r) << tbits;
+	double *q_out = cfg.q_out;
+	const double phi = cfg.phi;
+	(void)q_out;
+	// Phase A: pairs (x, x + 1) with x = map_a(tid, 2 i); register bits
+	// {0, 10, 11, 12}.  Reads the tile from the bulk-copied buffer (or the
+	// prior tables), applies the update, writes q'.
+	double v[kPerThread];
+	float f = 0.0f;
+	int hmax = 0;
+#pragma unroll
+	for (int i = 0; i < kPerThread / 2; i++)
+	{
+		const unsigned int x = map_a(tid, 2 * i);
+		double2 p = make_double2(0.0, 0.0);
+		if (x < tsize)
+		{
+			if (kMode == kGenerate)
 			{
-				const int st = L.stage;
-				if (L.out_pos)
-					L.out_pos[st - 1] = L.pos;
-				if (L.out_neg)
-					L.out_neg[st - 1] = L.neg;
-				if (st >= L.stages)
-					L.sess_active = 0;
+				const double2 lo = *reinterpret_cast<const double2 *>(cfg.prior_lo + x);
+				p = make_double2(phi * lo.x, phi * lo.y);
+			}
+			else
+			{
+				p = *reinterpret_cast<const double2 *>(in + x);
+			}
+			if (kMode == kUpdate)
+			{
+				const unsigned int s0 = static_cast<unsigned int>(base) | x;
+				if (cfg.dilution_classes)
+				{
+					p.x *= ps.ctab[__popc(e & s0)];
+					p.y *= ps.ctab[__popc(e & (s0 | 1u))];
+				}
+				else
+				{
+					p.x *= (e & s0) == e ? cfg.c_in : cfg.c_out;
+					p.y *= (e & (s0 | 1u)) == e ? cfg.c_in : cfg.c_out;
+				}
+			}
+			if (kMode != kLoad)
+				*reinterpret_cast<double2 *>(in + x) = p; // q', bulk-stored by the caller
+		}
+		v[2 * i] = p.x;
+		v[2 * i + 1] = p.y;
+		f += approx_scaled_hi(p.x) + approx_scaled_hi(p.y);
+		hmax = max(hmax, max(__double2hiint(p.x), __double2hiint(p.y)));
+	}
+	if (hmax >= 0x7FF00000)
+		ps.flag = 1;
+	if (kMode != kLoad)
+		proxy_fence(); // q' in shared memory -> visible to the bulk store
+	const float est = block_sum(f, ps.fred, abort);
+	if (abort)
+		return true;
+	if (kMode != kLoad && threadIdx.x == 0)
+	{
+		bulk_store(q_out + base, in, static_cast<uint32_t>(sizeof(double)) << tbits);
+		bulk_commit();
+	}
+	// Scale so that the tile total lands in [2^61, 2^62 (1 + 2^-20)).
+	const int ef = (__float_as_int(est) >> 23) & 0xFF;
+	const int scale = ef == 0 ? 238 : 252 - ef;
+	u64 a[kPerThread];
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		a[j] = to_fixed_fast(v[j], scale);
+	const unsigned int mask = tsize - 1u;
+	levels_a(a, mask);
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		work[tile_swz(map_a(tid, j))] = a[j];
+	__syncthreads();
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		a[j] = work[tile_swz(map_b(tid, j))];
+	levels_b(a, mask);
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		work[tile_swz(map_b(tid, j))] = a[j];
+	__syncthreads();
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		a[j] = work[tile_swz(map_c(tid, j))];
+	levels_c(a, mask);
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		work[tile_swz(map_c(tid, j))] = a[j];
+	__syncthreads();
+	// Phase D: thread t holds columns 16 t .. 16 t + 15; tile bit 1 remains.
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+		a[j] = work[tile_swz(map_d(tid, j))];
+	reg_level(a, 1, 1, mask);
+	const unsigned int rows = 1u << cfg.hbits;
+	const int colw = cfg.colw, logw = cfg.logw;
+	const unsigned int c0 = tid << 4;
+	if (c0 < tsize)
+	{
+		if (colw >= 4)
+		{
+			// Column chunks of W >= 4 values: one full 32-byte sector per store.
+#pragma unroll
+			for (int j = 0; j < kPerThread; j += 4)
+			{
+				const unsigned int col = c0 + j;
+				if (col < tsize)
+				{
+					u64 *dst = cfg.m1 + (static_cast<size_t>(col >> logw) * rows + r) * colw + (col & (colw - 1));
+					st_global_v4_u64(dst, a[j], a[j + 1], a[j + 2], a[j + 3]);
+				}
 			}
 		}
-		L.k1_count = 0;
+		else
+		{
+#pragma unroll
+			for (int j = 0; j < kPerThread; j += 2)
+			{
+				const unsigned int col = c0 + j;
+				if (col < tsize)
+				{
+					u64 *dst = cfg.m1 + (static_cast<size_t>(col >> logw) * rows + r) * colw + (col & (colw - 1));
+					*reinterpret_cast<ulonglong2 *>(dst) = make_ulonglong2(a[j], a[j + 1]);
+				}
+			}
+		}
+	}
+	total_out = a[0];
+	scale_out = scale;
+	return false;
+}
+
+// Loads the per-lattice constants of lattice li into ps.lc (warp 0), the
+// likelihood-class table included for updates.
+__device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
+{
+	const unsigned int tid = threadIdx.x;
+	if (tid < 32)
+	{
+		const int mode = L.mode;
+		const unsigned int e = L.pend_e;
+		if (mode == kUpdate)
+		{
+			const int pool = __popc(e);
+			ps.ctab[tid] = static_cast<int>(tid) <= pool
+							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1) / L.z_norm
+							   : 0.0;
+		}
+		__syncwarp();
+		if (tid == 0)
+		{
+			LatCache &c = ps.lc;
+			c.li = li;
+			c.mode = mode;
+			c.e = e;
+			c.tbits = L.tbits;
+			c.hbits = L.hbits;
+			c.colw = L.colw;
+			c.logw = L.logw;
+			c.dilution = L.dilution;
+			c.skip = L.skip;
+			c.n = L.n;
+			c.active = L.active;
+			c.q_in = L.q_in;
+			c.q_out = L.q_out;
+			c.m1 = L.m1;
+			c.prior_lo = L.prior_lo;
+			c.prior_hi = L.prior_hi;
+			c.zg = L.z_g;
+			c.masses = L.masses_in_k2;
+			c.tile_total = L.tile_total;
+			c.tile_scale = L.tile_scale;
+			c.c_in = mode == kUpdate ? ps.ctab[__popc(e)] : 0.0;
+			c.c_out = mode == kUpdate ? ps.ctab[0] : 0.0;
+		}
+	}
+}
+
+// K1: [update] -> per-tile fixed point -> zeta over the low t bits -> M1.
+// Grid: persistent, at most one CTA per work item; `per` = tiles per lattice.
+__global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, int count, int per)
+{
+	double *const inbuf0 = tile_f64(0);
+	double *const inbuf1 = tile_f64(1);
+	const unsigned int tid = threadIdx.x;
+	const long long total = static_cast<long long>(count) * per;
+	long long w = blockIdx.x;
+	if (w >= total)
+		return;
+	if (tid == 0)
+	{
+		mbar_init(&ps.bars[0], 1);
+		mbar_init(&ps.bars[1], 1);
+		mbar_init_fence();
+		ps.flag = 0;
+	}
+	load_lattice_cache(states[w / per], static_cast<int>(w / per));
+	__syncthreads();
+	// Thread 0 issues the bulk copy of item `item` into buffer b (no copy
+	// for generated priors); same-lattice items use the cached constants.
+	auto issue = [&](long long item, int b) -> bool {
+		const int li = static_cast<int>(item / per);
+		const unsigned int rn = static_cast<unsigned int>(item % per);
+		int mode, tbits;
+		const double *q_in;
+		if (li == ps.lc.li)
+		{
+			mode = ps.lc.mode;
+			tbits = ps.lc.tbits;
+			q_in = ps.lc.q_in;
+		}
+		else
+		{
+			const LatticeDev &Ln = states[li];
+			mode = Ln.mode;
+			tbits = Ln.tbits;
+			q_in = Ln.q_in;
+		}
+		if (mode == kGenerate)
+			return false;
+		const uint32_t bytes = 8u << tbits;
+		mbar_expect_tx(&ps.bars[b], bytes);
+		bulk_load(b ? inbuf1 : inbuf0, q_in + (static_cast<size_t>(rn) << tbits), bytes, &ps.bars[b]);
+		return true;
+	};
+	uint32_t parity0 = 0u, parity1 = 0u;
+	bool inflight0 = false, inflight1 = false; // meaningful in thread 0 only
+	if (tid == 0)
+		inflight0 = issue(w, 0);
+	int done = 0; // items of the cached lattice finished by this CTA, not yet counted
+	for (int it = 0; w < total; w += gridDim.x, it++)
+	{
+		const int b = it & 1;
+		const int li = static_cast<int>(w / per);
+		const unsigned int r = static_cast<unsigned int>(w % per);
+		if (li != ps.lc.li)
+		{
+			__syncthreads();
+			load_lattice_cache(states[li], li);
+			__syncthreads();
+		}
+		const int mode = ps.lc.mode;
+		const long long wn = w + gridDim.x;
+		if (tid == 0 && wn < total)
+		{
+			// Buffer b ^ 1 may still be the source of the previous tile's q'
+			// bulk store.
+			bulk_wait_read_all();
+			proxy_fence();
+			if (b)
+				inflight0 = issue(wn, 0);
+			else
+				inflight1 = issue(wn, 1);
+		}
+		bool timed_out = false;
+		if (mode != kGenerate)
+		{
+			timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);
+			if (b)
+				parity1 ^= 1u;
+			else
+				parity0 ^= 1u;
+		}
+		if (tid == 0)
+		{
+			if (b)
+				inflight1 = false;
+			else
+				inflight0 = false;
+		}
+		ItemCfg cfg;
+		cfg.q_out = ps.lc.q_out;
+		cfg.m1 = ps.lc.m1;
+		cfg.prior_lo = ps.lc.prior_lo;
+		cfg.phi = mode == kGenerate ? ps.lc.prior_hi[r] : 0.0;
+		cfg.e = ps.lc.e;
+		cfg.tbits = ps.lc.tbits;
+		cfg.hbits = ps.lc.hbits;
+		cfg.colw = ps.lc.colw;
+		cfg.logw = ps.lc.logw;
+		cfg.dilution_classes = ps.lc.dilution;
+		cfg.c_in = ps.lc.c_in;
+		cfg.c_out = ps.lc.c_out;
+		u64 tile_total = 0;
+		int tile_scale = 0;
+		bool abort;
+		if (mode == kUpdate)
+			abort = k1_item<kUpdate>(cfg, r, b, timed_out, tile_total, tile_scale);
+		else if (mode == kGenerate)
+			abort = k1_item<kGenerate>(cfg, r, b, timed_out, tile_total, tile_scale);
+		else
+			abort = k1_item<kLoad>(cfg, r, b, timed_out, tile_total, tile_scale);
+		if (abort)
+		{
+			if (tid == 0)
+			{
+				atomicExch(&states[li].error, kErrTimeout);
+				if (b ? inflight0 : inflight1)
+					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
+				bulk_wait_all();
+			}
+			return;
+		}
+		if (tid == 0)
+		{
+			ps.lc.tile_total[r] = tile_total;
+			ps.lc.tile_scale[r] = tile_scale;
+		}
+		done++;
+		// Count this CTA's finished items of the lattice when it moves on to
+		// another lattice or runs out of work; the CTA completing the
+		// lattice runs its epilogue.
+		if (wn >= total || static_cast<int>(wn / per) != li)
+		{
+			LatticeDev &L = states[li];
+			__syncthreads();
+			if (tid == 0)
+			{
+				if (ps.flag)
+					atomicExch(&L.error, kErrNonFinite);
+				ps.flag = 0;
+				bulk_wait_all(); // this lattice's q' stores are complete
+				__threadfence();
+				ps.last = atomicAdd(&L.k1_count, static_cast<unsigned int>(done)) ==
+						  static_cast<unsigned int>(per - done);
+			}
+			done = 0;
+			__syncthreads();
+			if (ps.last)
+			{
+				__threadfence();
+				k1_epilogue(L, mode);
+			}
+		}
 	}
 }
 
 // ------------------------------------------------------------------ K2
 
-__device__ __forceinline__ void argmin_warp(unsigned long long &s, unsigned int &e)
+// K2 epilogue of lattice L: the block winners' argmin and, in session mode,
+// classification, the drawn response and the queued update.
+__device__ void k2_epilogue(LatticeDev &L, int per)
 {
-	for (int o = 16; o > 0; o >>= 1)
-	{
-		const unsigned long long os = __shfl_xor_sync(0xFFFFFFFFu, s, o);
-		const unsigned int oe = __shfl_xor_sync(0xFFFFFFFFu, e, o);
-		if (better(os, oe, s, e))
-		{
-			s = os;
-			e = oe;
-		}
-	}
-}
-
-// One K2 column block: see the header.  Dynamic shared memory:
-// 2^hbits * 16 u64 plus 2^hbits ints.
-__global__ void __launch_bounds__(kHighThreads, 1) k2_zeta_high_select(LatticeDev *states)
-{
-	extern __shared__ unsigned long long sm[];
-	LatticeDev &L = states[blockIdx.y];
-	if (L.skip)
-		return;
-	const int tid = threadIdx.x;
-	const int tbits = L.tbits, hbits = L.hbits;
-	const unsigned int rows = 1u << hbits;
-	const unsigned int b = blockIdx.x;
-	int *shift = reinterpret_cast<int *>(sm + static_cast<size_t>(rows) * kColW);
-	const int s_g = L.s_g;
-	for (unsigned int rr = tid; rr < rows; rr += kHighThreads)
-		shift[rr] = s_g - L.tile_scale[rr];
-	__syncthreads();
-
-	const unsigned int c = tid & 15;
-	const unsigned int g = tid >> 4; // 0..31
-	unsigned long long a[32];
-	const unsigned long long *src = L.m1 + static_cast<size_t>(b) * rows * kColW;
-	// Phase 1: rows g + 32 i (row bits 5..9 in registers).
-#pragma unroll
-	for (int i = 0; i < 32; i++)
-	{
-		const unsigned int rr = g + 32u * i;
-		a[i] = rr < rows ? rescale(src[rr * kColW + c], shift[rr]) : 0ull;
-	}
-#pragma unroll
-	for (int lvl = 0; lvl < 5; lvl++)
-	{
-		if (5 + lvl < hbits)
-		{
-#pragma unroll
-			for (int i = 0; i < 32; i++)
-				if (!(i & (1 << lvl)))
-					a[i] += a[i | (1 << lvl)];
-		}
-	}
-#pragma unroll
-	for (int i = 0; i < 32; i++)
-	{
-		const unsigned int rr = g + 32u * i;
-		if (rr < rows)
-			sm[rr * kColW + c] = a[i];
-	}
-	__syncthreads();
-	// Phase 2: rows 32 g + i (row bits 0..4 in registers), then score.
-#pragma unroll
-	for (int i = 0; i < 32; i++)
-	{
-		const unsigned int rr = 32u * g + i;
-		a[i] = rr < rows ? sm[rr * kColW + c] : 0ull;
-	}
-#pragma unroll
-	for (int lvl = 0; lvl < 5; lvl++)
-	{
-		if (lvl < hbits)
-		{
-#pragma unroll
-			for (int i = 0; i < 32; i++)
-				if (!(i & (1 << lvl)))
-					a[i] += a[i | (1 << lvl)];
-		}
-	}
-	const unsigned int e_lo = b * kColW + c;
-	const unsigned long long zg = L.z_g;
-	const unsigned int active = L.active;
-	unsigned long long best = ~0ull;
-	unsigned int best_e = 0xFFFFFFFFu;
-	if (e_lo < (1u << tbits))
-	{
-#pragma unroll
-		for (int i = 0; i < 32; i++)
-		{
-			const unsigned int rr = 32u * g + i;
-			if (rr < rows)
-			{
-				const unsigned int E = (rr << tbits) | e_lo;
-				const unsigned long long m2 = a[i] << 1;
-				const unsigned long long score = m2 > zg ? m2 - zg : zg - m2;
-				if ((E & ~active) == 0 && better(score, E, best, best_e))
-				{
-					best = score;
-					best_e = E;
-				}
-			}
-		}
-	}
-	argmin_warp(best, best_e);
-	__shared__ unsigned long long wsc[kHighThreads / 32];
-	__shared__ unsigned int wse[kHighThreads / 32];
-	if ((tid & 31) == 0)
-	{
-		wsc[tid >> 5] = best;
-		wse[tid >> 5] = best_e;
-	}
-	__syncthreads();
-	__shared__ bool s_last;
-	if (tid < 32)
-	{
-		unsigned long long s2 = tid < kHighThreads / 32 ? wsc[tid] : ~0ull;
-		unsigned int e2 = tid < kHighThreads / 32 ? wse[tid] : 0xFFFFFFFFu;
-		argmin_warp(s2, e2);
-		if (tid == 0)
-		{
-			L.blk_score[b] = s2;
-			L.blk_e[b] = e2;
-			__threadfence();
-			const unsigned int prev = atomicAdd(&L.k2_count, 1u);
-			s_last = prev == gridDim.x - 1;
-		}
-	}
-	__syncthreads();
-	if (!s_last)
-		return;
-	__threadfence();
-	unsigned long long bs = ~0ull;
+	u64 bs = ~0ull;
 	unsigned int be = 0xFFFFFFFFu;
-	for (int i = tid; i < static_cast<int>(gridDim.x); i += kHighThreads)
+	for (int i = threadIdx.x; i < per; i += kThreads)
 	{
-		const unsigned long long s2 = __ldcg(L.blk_score + i);
+		const u64 s2 = __ldcg(L.blk_score + i);
 		const unsigned int e2 = __ldcg(L.blk_e + i);
 		if (better(s2, e2, bs, be))
 		{
@@ -465,43 +675,269 @@ __global__ void __launch_bounds__(kHighThreads, 1) k2_zeta_high_select(LatticeDe
 			be = e2;
 		}
 	}
-	argmin_warp(bs, be);
 	__syncthreads();
-	if ((tid & 31) == 0)
+	argmin_block(bs, be, ps.ws, ps.we);
+	if (threadIdx.x == 0)
 	{
-		wsc[tid >> 5] = bs;
-		wse[tid >> 5] = be;
+		L.best_score = bs;
+		L.best_e = be;
+		if (L.sess_active)
+		{
+			// Session stage (bgt::Lattice order: select -> update -> classify):
+			// classify the posterior the previous update produced, then queue
+			// this stage's update.
+			const int st = L.stage;
+			if (st > 0)
+			{
+				classify_atoms(L, L.up, L.lo);
+				if (L.out_pos)
+					L.out_pos[st - 1] = L.pos;
+				if (L.out_neg)
+					L.out_neg[st - 1] = L.neg;
+			}
+			if (st < L.stages)
+			{
+				const unsigned int rsp = bgt_session_sample_response(L.dilution, L.n, L.k, be, L.truth, L.alpha, L.hpar,
+																	 L.seed, L.session, static_cast<uint32_t>(st));
+				if (L.out_e)
+					L.out_e[st] = be;
+				if (L.out_r)
+					L.out_r[st] = rsp;
+				L.pend_e = be;
+				L.pend_r = rsp;
+				L.mode = kUpdate;
+				L.stage = st + 1;
+			}
+			else
+			{
+				L.sess_active = 0;
+			}
+		}
+		L.k2_count = 0;
 	}
 	__syncthreads();
-	if (tid < 32)
+}
+
+// K2: one W-column block of M1 (all 2^h rows, contiguous) per work item.
+__global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *states, int count, int per)
+{
+	u64 *const inbuf0 = tile_u64(0);
+	u64 *const inbuf1 = tile_u64(1);
+	u64 *const work = work_tile();
+	int *const shift = g_shift;
+	const unsigned int tid = threadIdx.x;
+	const long long total = static_cast<long long>(count) * per;
+	long long w = blockIdx.x;
+	if (w >= total)
+		return;
+	if (tid == 0)
 	{
-		unsigned long long s2 = tid < kHighThreads / 32 ? wsc[tid] : ~0ull;
-		unsigned int e2 = tid < kHighThreads / 32 ? wse[tid] : 0xFFFFFFFFu;
-		argmin_warp(s2, e2);
+		mbar_init(&ps.bars[0], 1);
+		mbar_init(&ps.bars[1], 1);
+		mbar_init_fence();
+		ps.lc.li = -1;
+	}
+	__syncthreads();
+	auto issue = [&](long long item, int b) -> bool {
+		const int li = static_cast<int>(item / per);
+		const unsigned int blk = static_cast<unsigned int>(item % per);
+		int skip, hbits, colw;
+		u64 *m1;
+		if (li == ps.lc.li)
+		{
+			skip = ps.lc.skip;
+			hbits = ps.lc.hbits;
+			colw = ps.lc.colw;
+			m1 = ps.lc.m1;
+		}
+		else
+		{
+			const LatticeDev &Ln = states[li];
+			skip = Ln.skip;
+			hbits = Ln.hbits;
+			colw = Ln.colw;
+			m1 = Ln.m1;
+		}
+		if (skip)
+			return false;
+		const uint32_t elems = (1u << hbits) * static_cast<uint32_t>(colw);
+		const uint32_t bytes = elems * 8u;
+		mbar_expect_tx(&ps.bars[b], bytes);
+		bulk_load(b ? inbuf1 : inbuf0, m1 + static_cast<size_t>(blk) * elems, bytes, &ps.bars[b]);
+		return true;
+	};
+	uint32_t parity0 = 0u, parity1 = 0u;
+	bool inflight0 = false, inflight1 = false;
+	if (tid == 0)
+		inflight0 = issue(w, 0);
+	int done = 0;
+	for (int it = 0; w < total; w += gridDim.x, it++)
+	{
+		const int b = it & 1;
+		const int li = static_cast<int>(w / per);
+		const unsigned int blk = static_cast<unsigned int>(w % per);
+		if (li != ps.lc.li)
+		{
+			__syncthreads();
+			const LatticeDev &Lc = states[li];
+			load_lattice_cache(Lc, li);
+			const int s_g = Lc.s_g;
+			const unsigned int rows_c = 1u << Lc.hbits;
+			for (unsigned int rr = tid; rr < rows_c; rr += kThreads)
+				shift[rr] = min(Lc.tile_scale[rr] - s_g, 63);
+			__syncthreads();
+		}
+		const long long wn = w + gridDim.x;
+		if (tid == 0 && wn < total)
+		{
+			proxy_fence();
+			if (b)
+				inflight0 = issue(wn, 0);
+			else
+				inflight1 = issue(wn, 1);
+		}
+		if (ps.lc.skip)
+			continue;
+		const int tbits = ps.lc.tbits, logw = ps.lc.logw;
+		const unsigned int rows = 1u << ps.lc.hbits;
+		const unsigned int elems = rows << logw;
+		const u64 zg = ps.lc.zg;
+		const unsigned int active = ps.lc.active;
+		const unsigned int all = ps.lc.n >= 32 ? 0xFFFFFFFFu : ((1u << ps.lc.n) - 1u);
+		const bool want_masses = ps.lc.masses != 0 && (blk & (blk - 1u)) == 0;
+		const bool timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);
+		if (b)
+			parity1 ^= 1u;
+		else
+			parity0 ^= 1u;
 		if (tid == 0)
 		{
-			__threadfence();
-			L.best_score = s2;
-			L.best_e = e2;
-			L.k2_count = 0;
-			if (L.sess_active)
+			if (b)
+				inflight1 = false;
+			else
+				inflight0 = false;
+		}
+		// Row bits of the block index y = row * W + column.
+		const unsigned int mask = (rows - 1u) << logw;
+		const u64 *in = b ? inbuf1 : inbuf0;
+		u64 a[kPerThread];
+#pragma unroll
+		for (int i = 0; i < kPerThread / 2; i++)
+		{
+			const unsigned int y = map_a(tid, 2 * i);
+			ulonglong2 p = make_ulonglong2(0ull, 0ull);
+			if (y < elems)
 			{
-				// Session step (bgt::Lattice order: select -> update -> classify).
-				const int st = L.stage;
-				if (st < L.stages)
-				{
-					const unsigned int r = bgt_session_sample_response(L.dilution, L.n, L.k, e2, L.truth, L.alpha,
-																	   L.hpar, L.seed, L.session,
-																	   static_cast<uint32_t>(st));
-					if (L.out_e)
-						L.out_e[st] = e2;
-					if (L.out_r)
-						L.out_r[st] = r;
-					L.pend_e = e2;
-					L.pend_r = r;
-					L.mode = kUpdate;
-					L.stage = st + 1;
-				}
+				p = *reinterpret_cast<const ulonglong2 *>(in + y);
+				const int rs = shift[y >> logw];
+				p.x = shr_round(p.x, rs);
+				p.y = shr_round(p.y, rs);
+			}
+			a[2 * i] = p.x;
+			a[2 * i + 1] = p.y;
+		}
+		levels_a(a, mask);
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			work[tile_swz(map_a(tid, j))] = a[j];
+		if (__syncthreads_or(timed_out))
+		{
+			if (tid == 0)
+			{
+				atomicExch(&states[li].error, kErrTimeout);
+				if (b ? inflight0 : inflight1)
+					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
+			}
+			return;
+		}
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			a[j] = work[tile_swz(map_b(tid, j))];
+		levels_b(a, mask);
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			work[tile_swz(map_b(tid, j))] = a[j];
+		__syncthreads();
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			a[j] = work[tile_swz(map_c(tid, j))];
+		levels_c(a, mask);
+		// All row bits are done (W >= 4, so y bits 0..1 are column bits).
+		// Score |2 M(E) - Z_g|; within a thread E grows with j, so a strict
+		// comparison keeps the lowest index on ties.
+		const unsigned int col_base = blk << logw;
+		const unsigned int wmask = (1u << logw) - 1u;
+		const unsigned int y0 = map_c(tid, 0);
+		u64 best = ~0ull;
+		int best_j = -1;
+		if ((active & all) == all)
+		{
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+			{
+				const u64 m2 = a[j] << 1;
+				const u64 score = m2 > zg ? m2 - zg : zg - m2;
+				const bool take = (y0 + (j << 2)) < elems && score < best;
+				best = take ? score : best;
+				best_j = take ? j : best_j;
+			}
+		}
+		else
+		{
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+			{
+				const unsigned int y = y0 + (j << 2);
+				const unsigned int E = ((y >> logw) << tbits) | col_base | (y & wmask);
+				const u64 m2 = a[j] << 1;
+				const u64 score = m2 > zg ? m2 - zg : zg - m2;
+				const bool take = y < elems && (E & ~active) == 0 && score < best;
+				best = take ? score : best;
+				best_j = take ? j : best_j;
+			}
+		}
+		unsigned int best_e = 0xFFFFFFFFu;
+		if (best_j >= 0)
+		{
+			const unsigned int y = y0 + (best_j << 2);
+			best_e = ((y >> logw) << tbits) | col_base | (y & wmask);
+		}
+		LatticeDev &L = states[li];
+		// Singleton (atom) masses live in block 0 and in the blocks whose
+		// first column is a power of two.
+		if (want_masses)
+		{
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+			{
+				const unsigned int y = y0 + (j << 2);
+				const unsigned int E = ((y >> logw) << tbits) | col_base | (y & wmask);
+				if (y < elems && __popc(E) == 1)
+					L.atom_fixed[__ffs(E) - 1] = a[j];
+			}
+		}
+		argmin_block(best, best_e, ps.ws, ps.we);
+		if (tid == 0)
+		{
+			L.blk_score[blk] = best;
+			L.blk_e[blk] = best_e;
+		}
+		done++;
+		if (wn >= total || static_cast<int>(wn / per) != li)
+		{
+			__syncthreads();
+			if (tid == 0)
+			{
+				__threadfence();
+				ps.last = atomicAdd(&L.k2_count, static_cast<unsigned int>(done)) ==
+						  static_cast<unsigned int>(per - done);
+			}
+			done = 0;
+			__syncthreads();
+			if (ps.last)
+			{
+				__threadfence();
+				k2_epilogue(L, per);
 			}
 		}
 	}
@@ -534,19 +970,18 @@ __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo
 
 // Exact fixed-point upset mass sum_{s superset of e} q[s] at the lattice's
 // global scale (for Lattice::upset_probability_mass).
-__global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, unsigned long long *out)
+__global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, u64 *out)
 {
 	const LatticeDev &L = *state;
 	const unsigned int free_bits = ~e & ((L.atoms >= 32) ? 0xFFFFFFFFu : ((1u << L.atoms) - 1u));
 	const int nfree = __popc(free_bits);
-	const unsigned long long count = 1ull << nfree;
-	unsigned long long acc = 0;
-	for (unsigned long long j = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; j < count;
-		 j += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+	const u64 count = 1ull << nfree;
+	u64 acc = 0;
+	for (u64 j = blockIdx.x * static_cast<u64>(blockDim.x) + threadIdx.x; j < count;
+		 j += static_cast<u64>(gridDim.x) * blockDim.x)
 	{
-		// Deposit the bits of j into the free positions.
 		unsigned int s = e, fb = free_bits;
-		unsigned long long jj = j;
+		u64 jj = j;
 		while (fb)
 		{
 			const unsigned int low = fb & (0u - fb);

@@ -18,16 +18,19 @@
 // of each input to fixed point.
 //
 // Stage structure for one binary (k = 1) lattice of n subjects, N = 2^n:
-//   K1 zeta_low   one CTA per tile of 2^t states (t = min(n, 14)):
+//   K1 zeta_low   tiles of 2^t states (t = min(n, 13)), persistent CTAs fed
+//                 by bulk (TMA) copies double-buffered on mbarriers:
 //                 [apply pending update q *= L/Z] -> q (FP64, written back)
 //                 -> u64 at a per-tile scale -> zeta over the t low bits
-//                 -> column-block-major partial sums M1 + tile totals.
+//                 -> partial sums M1 stored column-block-major (W columns
+//                 per block, all rows of a block contiguous) + tile totals.
 //                 The last CTA to finish derives the global scale and the
 //                 exact fixed-point total Z_g.
 //                 It also forms the exact atom marginals (low atoms from the
 //                 singleton columns of M1, high atoms from the tile totals)
 //                 and, after an update, classifies the atoms.
-//   K2 zeta_high  one CTA per 16-column block of M1: rescale to the global
+//   K2 zeta_high  one contiguous W-column block of M1 per work item (bulk
+//                 copied, double-buffered): rescale to the global
 //                 scale, zeta over the h = n - t high bits, exact score
 //                 |2 M(E) - Z_g| (Op-BHA; Op-BBPA for k = 1 is the same
 //                 ordering in exact arithmetic) over the experiments inside
@@ -44,14 +47,17 @@
 namespace bgt_gpu
 {
 
-constexpr int kTileBits = 14;                 // states per K1 tile = 2^14
-constexpr int kTileThreads = 1024;            // 16 states per thread
-constexpr int kPerThread = (1 << kTileBits) / kTileThreads;
-constexpr int kColW = 16;                     // K2 column block: 16 u64 = 128 B per row
-constexpr int kMaxHighBits = 10;              // K2 holds up to 2^10 rows x 16 columns (128 KB)
-constexpr int kHighThreads = 512;
+constexpr int kTileBits = 13;                 // states per K1 tile = 2^13 (64 KB of FP64)
+constexpr int kTileElems = 1 << kTileBits;
+constexpr int kThreads = 512;                 // both passes: 512 threads x 16 values
+constexpr int kPerThread = kTileElems / kThreads;
+constexpr int kMaxColW = 16;                  // K2 block columns (u64 values per M1 row chunk)
+constexpr int kMinColW = 4;                   // 32-byte row chunks at the least
+constexpr int kMaxHighBits = 11;              // K2 block = 2^h rows x W columns <= 2^13 values
 constexpr int kMaxAtoms = 30;
 constexpr int kMaxClasses = 32;               // likelihood classes for k = 1 (popcount 0..n)
+constexpr int kSmemBuf = kTileElems * 8;      // one 64 KB tile buffer
+constexpr int kPipeSmem = 3 * kSmemBuf;       // two bulk-copy buffers + one work buffer
 
 // Modes of K1.
 enum K1Mode : int
@@ -69,7 +75,9 @@ struct LatticeDev
 	int atoms;    // n * k
 	int tbits;    // low bits handled in K1 tiles
 	int hbits;    // high bits handled in K2
-	int nblk;     // K2 column blocks (max(1, 2^tbits / 16))
+	int nblk;     // K2 column blocks (2^tbits / colw)
+	int colw;     // K2 block columns W
+	int logw;     // log2(W)
 	int dilution; // 0 / 1
 	int orig_n;   // subjects of the dilution table
 	// ---- buffers (host-set) ----
@@ -94,10 +102,11 @@ struct LatticeDev
 	unsigned long long best_score;
 	unsigned long long atom_fixed[32];
 	unsigned int pos, neg;         // classification masks (internal order)
-	int classify_on_update;        // K1 classifies after applying an update (tree/session)
+	int classify_on_update;        // K1 classifies after applying an update (tree)
+	int masses_in_k2;              // K2 records the singleton (atom) masses (sessions)
 	int skip;                      // K2 leaves this lattice alone (tree leaves)
 	int error;                     // nonzero: a kernel detected a failure
-	unsigned int k1_count, k2_count; // last-CTA counters (reset by the last CTA)
+	unsigned int k1_count, k2_count; // completed work items (reset by the lattice's epilogue)
 	// ---- session (device-driven loop) ----
 	int sess_active;
 	int stage, stages;
@@ -111,12 +120,22 @@ enum LatticeError : int
 {
 	kErrNone = 0,
 	kErrZeroMass = 1,   // normalising constant is zero
-	kErrNonFinite = 2   // a non-finite posterior value was seen
+	kErrNonFinite = 2,  // a non-finite posterior value was seen
+	kErrTimeout = 3     // a bounded wait on a bulk copy expired
 };
 
 // ------------------------------------------------------------------ helpers
 
 __device__ __forceinline__ unsigned int tile_swz(unsigned int x) { return x ^ ((x >> 4) & 15u); }
+
+// v * 2^64 truncated to FP32 from the high word of the double (exponent and
+// top 20 mantissa bits), 0 below 2^-190.  Three integer operations.
+__device__ __forceinline__ float approx_scaled_hi(double v)
+{
+	const int hi = __double2hiint(v);
+	const int d = hi - (832 << 20);
+	return d <= 0 ? 0.0f : __int_as_float(static_cast<int>(static_cast<unsigned int>(d) << 3));
+}
 
 // v * 2^64 truncated to FP32 (never above the true value); 0 when below the
 // FP32 normal range.  Integer-only: no FP64 conversion instruction.
@@ -148,6 +167,26 @@ __device__ __forceinline__ unsigned long long to_fixed(double v, int scale)
 		return 0ull;
 	const int rs = -sh;
 	return (m + (1ull << (rs - 1))) >> rs;
+}
+
+// round-half-up(v * 2^scale) for finite v >= 0 with v * 2^scale < 2^63,
+// branch-free.  With m the 53-bit significand, v * 2^scale =
+// (m << 11) / 2^rs for rs = 1086 - exponent - scale >= 1; rs is clamped to
+// 64, where the result is already 0 or 1 unit.
+__device__ __forceinline__ unsigned long long to_fixed_fast(double v, int scale)
+{
+	const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+	const int e = static_cast<int>(b >> 52);
+	const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (static_cast<unsigned long long>(e != 0) << 52);
+	int rs = 1086 - scale - (e > 1 ? e : 1);
+	rs = rs < 1 ? 1 : (rs > 64 ? 64 : rs);
+	return (((m << 11) >> (rs - 1)) + 1ull) >> 1;
+}
+
+// round-half-up(v / 2^rs) for 0 <= rs <= 63 and v < 2^63, branch-free.
+__device__ __forceinline__ unsigned long long shr_round(unsigned long long v, int rs)
+{
+	return (((v << 1) >> rs) + 1ull) >> 1;
 }
 
 // round(v * 2^d) for a fixed-point value v.

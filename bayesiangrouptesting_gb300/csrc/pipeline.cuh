@@ -1,0 +1,110 @@
+// Asynchronous tile pipeline primitives for sm_103a: 1D bulk tensor-memory
+// copies (cp.async.bulk, the TMA engine) completing on shared-memory
+// mbarriers, with bounded waits.  Every wait gives up after a wall-clock
+// deadline so that a fault can never hang the GPU; callers turn a timeout
+// into an error status.
+#pragma once
+
+#include <cstdint>
+
+namespace bgt_gpu
+{
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+	return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Makes initialised barriers visible to the async (TMA) proxy.
+__device__ __forceinline__ void mbar_init_fence()
+{
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) accesses to the same memory.
+__device__ __forceinline__ void proxy_fence()
+{
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+				 : "memory");
+}
+
+// Global -> shared bulk copy of `bytes` (multiple of 16, both addresses
+// 16-byte aligned) that signals `bar` on completion.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+					 smem_u32(dst)),
+				 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+				 : "memory");
+}
+
+// Shared -> global bulk copy of `bytes` (multiple of 16, 16-byte aligned),
+// tracked by the issuing thread's bulk async-group.
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes)
+{
+	asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes)
+				 : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Waits until the issuing thread's committed bulk stores have finished
+// reading their shared-memory source (the buffer may then be reused).
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Waits until the issuing thread's committed bulk stores are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// One full 32-byte sector store (256-bit vector store; 32-byte aligned).
+__device__ __forceinline__ void st_global_v4_u64(unsigned long long *p, unsigned long long a, unsigned long long b,
+												 unsigned long long c, unsigned long long d)
+{
+	asm volatile("st.global.v4.u64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(a), "l"(b), "l"(c), "l"(d) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+	uint32_t ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+				 : "=r"(ok)
+				 : "r"(smem_u32(bar)), "r"(parity)
+				 : "memory");
+	return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Waits for phase `parity` of `bar` for at most ~2 s; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+	if (mbar_try_wait(bar, parity))
+		return true;
+	const uint64_t deadline = global_ns() + 2000000000ull;
+	for (uint32_t it = 0; it < (1u << 30); ++it)
+	{
+		if (mbar_try_wait(bar, parity))
+			return true;
+		if ((it & 63u) == 63u && global_ns() > deadline)
+			return false;
+	}
+	return false;
+}
+
+} // namespace bgt_gpu

@@ -21,7 +21,7 @@ struct CudaFailure : std::runtime_error
 
 struct LatticeGeometry
 {
-	int n = 0, k = 1, atoms = 0, tbits = 0, hbits = 0, nblk = 1;
+	int n = 0, k = 1, atoms = 0, tbits = 0, hbits = 0, nblk = 1, colw = 1, logw = 0;
 };
 
 void set_error(const std::string &message);
@@ -34,5 +34,6 @@ void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
 size_t k1_smem_bytes();
 size_t k2_smem_bytes(int hbits);
+int sm_count();
 
 } // namespace bgt_gpu

@@ -233,7 +233,7 @@ void allocate_level(Level &lv, const LatticeGeometry &g)
 	const size_t rows = size_t{1} << g.hbits;
 	cuda_check(cudaMalloc(&lv.states, count * sizeof(LatticeDev)), "alloc tree states");
 	cuda_check(cudaMalloc(&lv.q, count * states * sizeof(double)), "alloc tree posteriors");
-	cuda_check(cudaMalloc(&lv.m1, count * static_cast<size_t>(g.nblk) * rows * kColW * sizeof(unsigned long long)),
+	cuda_check(cudaMalloc(&lv.m1, count * static_cast<size_t>(g.nblk) * rows * g.colw * sizeof(unsigned long long)),
 			   "alloc tree zeta partials");
 	cuda_check(cudaMalloc(&lv.tile_total, count * rows * sizeof(unsigned long long)), "alloc tile totals");
 	cuda_check(cudaMalloc(&lv.tile_scale, count * rows * sizeof(int)), "alloc tile scales");
@@ -247,7 +247,7 @@ void bind_level_buffers(Level &lv, const LatticeGeometry &g, size_t i, LatticeDe
 	const size_t states = size_t{1} << g.atoms;
 	const size_t rows = size_t{1} << g.hbits;
 	d.q_out = lv.q + i * states;
-	d.m1 = lv.m1 + i * static_cast<size_t>(g.nblk) * rows * kColW;
+	d.m1 = lv.m1 + i * static_cast<size_t>(g.nblk) * rows * g.colw;
 	d.tile_total = lv.tile_total + i * rows;
 	d.tile_scale = lv.tile_scale + i * rows;
 	d.blk_score = lv.blk_score + i * g.nblk;
@@ -324,6 +324,9 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 		d.tbits = g.tbits;
 		d.hbits = g.hbits;
 		d.nblk = g.nblk;
+		d.colw = g.colw;
+		d.logw = g.logw;
+		d.masses_in_k2 = 0;
 		d.dilution = use_dilution;
 		d.orig_n = subjects;
 		d.dil = static_cast<double *>(d_dil.ptr);
