@@ -32,6 +32,65 @@ namespace
 {
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
+
+// Benchmark kernel timing (bgt_gpu_profile_*): event pairs per pass.
+struct PassTimer
+{
+	bool enabled = false;
+	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[2];
+	std::vector<cudaEvent_t> pool;
+	uint64_t launches[2] = {0, 0};
+	double ms[2] = {0.0, 0.0};
+
+	cudaEvent_t get()
+	{
+		if (!pool.empty())
+		{
+			cudaEvent_t e = pool.back();
+			pool.pop_back();
+			return e;
+		}
+		cudaEvent_t e = nullptr;
+		cuda_check(cudaEventCreate(&e), "event create");
+		return e;
+	}
+
+	void drain()
+	{
+		for (int p = 0; p < 2; p++)
+		{
+			for (auto &pr : pending[p])
+			{
+				cuda_check(cudaEventSynchronize(pr.second), "event sync");
+				float t = 0.0f;
+				cuda_check(cudaEventElapsedTime(&t, pr.first, pr.second), "event elapsed");
+				ms[p] += t;
+				launches[p]++;
+				pool.push_back(pr.first);
+				pool.push_back(pr.second);
+			}
+			pending[p].clear();
+		}
+	}
+};
+PassTimer g_timer;
+
+template <typename Launch>
+void timed_launch(int pass, cudaStream_t stream, Launch &&launch)
+{
+	if (!g_timer.enabled)
+	{
+		launch();
+		return;
+	}
+	cudaEvent_t a = g_timer.get(), b = g_timer.get();
+	cuda_check(cudaEventRecord(a, stream), "event record");
+	launch();
+	cuda_check(cudaEventRecord(b, stream), "event record");
+	g_timer.pending[pass].push_back({a, b});
+	if (g_timer.pending[pass].size() > 4096)
+		g_timer.drain();
+}
 } // namespace
 
 void set_error(const std::string &message) { g_last_error = message; }
@@ -76,7 +135,7 @@ void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 {
 	const long long items = static_cast<long long>(count) << g.hbits;
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
-	k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, count, 1 << g.hbits);
+	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, count, 1 << g.hbits); });
 	cuda_check(cudaGetLastError(), "k1 launch");
 	count_launches(1);
 }
@@ -85,7 +144,8 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 {
 	const long long items = static_cast<long long>(count) * g.nblk;
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
-	k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, count, g.nblk);
+	timed_launch(1, stream,
+				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, count, g.nblk); });
 	cuda_check(cudaGetLastError(), "k2 launch");
 	count_launches(1);
 }
@@ -298,6 +358,33 @@ uint64_t bgt_gpu_kernel_launch_count(void) { return g_launches.load(); }
 
 int bgt_cuda_provider_available(void) { return device_present() ? 1 : 0; }
 
+int bgt_gpu_profile_enable(int enable)
+{
+	return guarded([&]() -> int {
+		if (!enable)
+			g_timer.drain();
+		g_timer.enabled = enable != 0;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_profile_read(uint64_t *launches, double *milliseconds)
+{
+	return guarded([&]() -> int {
+		g_timer.drain();
+		for (int p = 0; p < 2; p++)
+		{
+			if (launches)
+				launches[p] = g_timer.launches[p];
+			if (milliseconds)
+				milliseconds[p] = g_timer.ms[p];
+			g_timer.launches[p] = 0;
+			g_timer.ms[p] = 0.0;
+		}
+		return BGT_GPU_OK;
+	});
+}
+
 int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const double *prior, int precision,
 						   bgt_gpu_lattice **out)
 {
@@ -399,6 +486,40 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			throw;
 		}
 		*out = lat;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_reset(bgt_gpu_lattice *lattice, const double *prior)
+{
+	if (!lattice || !prior)
+	{
+		set_error("null lattice or prior pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return guarded([&]() -> int {
+		const LatticeGeometry &g = lattice->g;
+		cuda_check(cudaMemcpyAsync(lattice->pi0, prior, g.atoms * sizeof(double), cudaMemcpyHostToDevice,
+								   lattice->stream),
+				   "prior upload");
+		const unsigned int rows = 1u << g.hbits;
+		const unsigned int span = std::max<unsigned int>(1u << g.tbits, rows);
+		prior_tables<<<(span + 255) / 256, 256, 0, lattice->stream>>>(lattice->pi0, g.atoms, g.tbits, lattice->prior_lo,
+																		lattice->prior_hi);
+		cuda_check(cudaGetLastError(), "prior tables launch");
+		count_launches(1);
+		LatticeDev &h = lattice->host;
+		h.q_in = lattice->q;
+		h.q_out = lattice->q;
+		h.mode = kGenerate;
+		h.z_norm = 1.0;
+		h.pos = h.neg = 0;
+		h.error = 0;
+		h.sess_active = 0;
+		h.k1_count = h.k2_count = 0;
+		cuda_check(cudaMemcpyAsync(lattice->dev, &h, sizeof(h), cudaMemcpyHostToDevice, lattice->stream), "state reset");
+		lattice->pos = lattice->neg = 0;
+		lattice->run_k1();
 		return BGT_GPU_OK;
 	});
 }

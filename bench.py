@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark of the lattice hot path: adaptive-testing sessions on a binary
+dilution lattice of 24 subjects (2^24 FP64 states, 128 MB), 32 stages of
+Op-BBPA selection -> update -> classification each.
+
+One step = one full session: the lattice is reset to a seeded prior
+(pi0 ~ U[0.005, 0.10]), a true state is drawn from that prior, and 32 stages
+run with each response drawn from DilutionTable(24, alpha=0.01, h=0.005)
+given the true state (include/bgt_session_rng.h).  The metric is lattice
+stages per second.
+
+Default (GB300) arm: the CUDA provider through its C ABI.  `--impl reference`
+times the reference algorithm on the host cores instead: the CPU oracle
+(a restatement of the reference CPU provider, oracle/bgt_oracle.c), one
+independent session per core.
+
+Prints one JSON line (rank 0).  Under torchrun each rank runs its own
+sessions on its own GPU (replicas; no collective on the data path) and the
+value is the whole-job aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+SUBJECTS = 24
+STAGES = 32
+ALPHA = 0.01
+H = 0.005
+PRIOR_LO, PRIOR_HI = 0.005, 0.10
+THRESHOLD = 0.01
+SEED = 20260624
+METRIC = "lattice stages/s"
+WORKLOAD = "binary dilution lattice n=24 (2^24 FP64 states), 32-stage Op-BBPA select->update->classify session"
+
+M64 = (1 << 64) - 1
+
+
+# -------------------------------------------------- workload (host copies of
+# the counter-based streams of include/bgt_session_rng.h)
+def _mix64(z: int) -> int:
+    z = (z + 0x9E3779B97F4A7C15) & M64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def _uniform(seed: int, session: int, tag: int, index: int) -> float:
+    key = _mix64(seed ^ _mix64((session + 0x632BE59BD9B4E019) & M64)) ^ _mix64((tag << 32) | index)
+    return (_mix64(key) >> 11) * (1.0 / 9007199254740992.0)
+
+
+def session_prior(seed: int, session: int, n: int = SUBJECTS) -> np.ndarray:
+    return np.array([PRIOR_LO + (PRIOR_HI - PRIOR_LO) * _uniform(seed, session, 1, i) for i in range(n)])
+
+
+def session_truth(seed: int, session: int, pi0: np.ndarray) -> int:
+    s = 0
+    for i, p in enumerate(pi0):
+        if not (_uniform(seed, session, 2, i) < p):
+            s |= 1 << i
+    return s
+
+
+# -------------------------------------------------- distributed helpers
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# -------------------------------------------------- clocks sampling
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.path = tempfile.mktemp(prefix="bgt_clocks_", suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# -------------------------------------------------- CPU baseline (oracle)
+def _oracle_worker(args):
+    session, stages = args
+    from oracle.oracle import Oracle
+
+    o = Oracle()
+    pi0 = session_prior(SEED, session)
+    truth = session_truth(SEED, session, pi0)
+    t0 = time.perf_counter()
+    o.session(1, SUBJECTS, 1, pi0, stages, SEED, session, truth, selector=2, alpha=ALPHA, h=H, up=THRESHOLD,
+              lo=THRESHOLD)
+    return stages, time.perf_counter() - t0
+
+
+def cpu_baseline(stages: int = 2, workers: int = 1):
+    """The oracle port timed on host cores: `workers` independent sessions of
+    `stages` stages each, in parallel processes.  Returns stages/s."""
+    from oracle.oracle import build_oracle
+
+    build_oracle()
+    ctx = mp.get_context("spawn")
+    jobs = [(10_000_000 + i, stages) for i in range(workers)]
+    t0 = time.perf_counter()
+    if workers == 1:
+        results = [_oracle_worker(jobs[0])]
+    else:
+        with ctx.Pool(workers) as pool:
+            results = pool.map(_oracle_worker, jobs)
+    wall = time.perf_counter() - t0
+    return sum(r[0] for r in results) / wall, wall
+
+
+def read_profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/k1_zeta_low_n24_session.md), or None."""
+    path = os.path.join(REPO, "profiles", "k1_zeta_low_n24_session.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def measured_peak_hbm():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            return float(json.load(open(path))["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+# -------------------------------------------------- arms
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    workers = max(1, os.cpu_count() or 1)
+    stages = args.ref_stages
+    for _ in range(args.warmup):
+        cpu_baseline(stages, workers)
+    values, walls = [], []
+    for _ in range(args.steps):
+        v, wall = cpu_baseline(stages, workers)
+        values.append(v)
+        walls.append(wall)
+    total_stages = stages * workers * args.steps
+    value = total_stages / sum(walls)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "stages/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "subjects": SUBJECTS, "stages": STAGES, "dilution_alpha": ALPHA,
+                   "dilution_h": H, "prior": [PRIOR_LO, PRIOR_HI], "sessions_per_step": workers,
+                   "stages_per_session_sample": stages},
+        "cpu_baseline": {"value": value, "unit": "stages/s", "cores": workers, "kind": "port",
+                         "sample": f"{workers} independent n=24 sessions x {stages} stages per step, one per core"},
+        "e2e": {"value": value, "unit": "stages/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+
+    from bayesiangrouptesting_gb300 import _native
+    from bayesiangrouptesting_gb300.build import build
+
+    build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = _native.load()
+    if not lib.bgt_cuda_provider_available():
+        raise SystemExit("no CUDA device")
+    dp = ctypes.POINTER(ctypes.c_double)
+    up = ctypes.POINTER(ctypes.c_uint32)
+    stream = torch.cuda.Stream()
+    # Pinned host buffers for the per-step inputs and outputs.
+    prior_h = torch.empty(SUBJECTS, dtype=torch.float64, pin_memory=True)
+    outs = [torch.empty(STAGES, dtype=torch.int32, pin_memory=True) for _ in range(4)]
+    handle = ctypes.c_void_p()
+    first = session_prior(SEED, rank << 32)
+    prior_h.copy_(torch.from_numpy(first))
+    _native.check(lib.bgt_gpu_lattice_create(1, SUBJECTS, 1, ctypes.cast(prior_h.data_ptr(), dp), 0,
+                                             ctypes.byref(handle)))
+    _native.check(lib.bgt_gpu_lattice_set_stream(handle, ctypes.c_void_p(stream.cuda_stream)))
+
+    def step(k: int):
+        session = (rank << 32) + k
+        pi0 = session_prior(SEED, session)
+        truth = session_truth(SEED, session, pi0)
+        prior_h.copy_(torch.from_numpy(pi0))
+        _native.check(lib.bgt_gpu_lattice_reset(handle, ctypes.cast(prior_h.data_ptr(), dp)))
+        _native.check(lib.bgt_gpu_session_run(handle, 2, STAGES, ALPHA, H, THRESHOLD, THRESHOLD, SEED, session,
+                                              truth, *[ctypes.cast(o.data_ptr(), up) for o in outs]))
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = _native.launches()
+    lib.bgt_gpu_profile_read(None, None)
+    lib.bgt_gpu_profile_enable(1)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    wall_steps = []
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        start.record(stream)
+        for k in range(args.steps):
+            t0 = time.perf_counter()
+            step(args.warmup + k)
+            wall_steps.append(time.perf_counter() - t0)
+        end.record(stream)
+        torch.cuda.synchronize()
+    lib.bgt_gpu_profile_enable(0)
+    kl = (ctypes.c_uint64 * 2)()
+    kms = (ctypes.c_double * 2)()
+    _native.check(lib.bgt_gpu_profile_read(kl, kms))
+    launches = _native.launches() - launches0
+    elapsed_ms = start.elapsed_time(end)
+    wall_ms = 1e3 * sum(wall_steps)
+    if world > 1:
+        t = torch.tensor([elapsed_ms, wall_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms, wall_ms = float(t[0]), float(t[1])
+    total_stages = STAGES * args.steps * world
+    value = total_stages / (elapsed_ms / 1e3)
+    e2e = total_stages / (wall_ms / 1e3)
+
+    n_states = 1 << SUBJECTS
+    # Dominant kernel: the update + low-bit zeta pass.  Algorithmic bytes per
+    # launch: read and write the 2^24 FP64 posterior (16 B per state) for the
+    # 32 update launches of a session, write it (8 B per state) for the prior.
+    k1_launches, k1_ms = int(kl[0]), float(kms[0])
+    per_session_bytes = STAGES * 16 * n_states + 8 * n_states
+    k1_alg_bytes = per_session_bytes * args.steps
+    achieved = k1_alg_bytes / (k1_ms / 1e3) / 1e9 if k1_ms > 0 else None
+    peak, peak_kind = measured_peak_hbm()
+    traffic = read_profile_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": traffic,
+                "kernel": "k1_zeta_low", "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": per_session_bytes / (STAGES + 1),
+                "kernel_ms_per_launch": k1_ms / max(1, k1_launches),
+                "select_pass_ms_per_launch": float(kms[1]) / max(1, int(kl[1])),
+                "select_pass_gbs": (8 * n_states * int(kl[1])) / (float(kms[1]) / 1e3) / 1e9 if kms[1] > 0 else None}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cv, cwall = cpu_baseline(stages=args.cpu_stages, workers=1)
+        cpu = {"value": cv, "unit": "stages/s", "cores": 1, "kind": "port",
+               "sample": f"one n=24 session, {args.cpu_stages} stages, oracle port on 1 core ({cwall:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "stages/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 storage, exact u64 fixed-point reductions",
+        "data": "synthetic (seeded priors, true states and responses)",
+        "config": {"workload": WORKLOAD, "subjects": SUBJECTS, "stages": STAGES, "dilution_alpha": ALPHA,
+                   "dilution_h": H, "prior": [PRIOR_LO, PRIOR_HI], "selector": "op_bbpa",
+                   "thresholds": [THRESHOLD, THRESHOLD], "parallelism": f"replicas{world}",
+                   "l2": "working set 256 MB (posterior + zeta partials) > 129 MB L2; no flush"},
+        "e2e": {"value": e2e, "unit": "stages/s", "h2d_bytes_per_step": 8 * SUBJECTS,
+                "d2h_bytes_per_step": 4 * 4 * STAGES},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lib.bgt_gpu_lattice_destroy(handle)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-stages", type=int, default=3, help="stages in the bounded CPU-baseline sample")
+    ap.add_argument("--ref-stages", type=int, default=2, help="stages per core per step in the reference arm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

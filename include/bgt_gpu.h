@@ -109,6 +109,11 @@ BGT_GPU_API int bgt_gpu_lattice_create(int lattice_type, int subjects, int varia
 									   int precision, bgt_gpu_lattice **out);
 BGT_GPU_API int bgt_gpu_lattice_destroy(bgt_gpu_lattice *lattice);
 
+/* Resets the lattice to the product prior of `prior` (subjects*variants
+ * prevalences), reusing its device memory: a new session can start without
+ * reallocating.  Classification masks are cleared. */
+BGT_GPU_API int bgt_gpu_lattice_reset(bgt_gpu_lattice *lattice, const double *prior);
+
 /* Launch all of this lattice's work on `stream` (a cudaStream_t); 0 restores
  * the lattice's own stream. */
 BGT_GPU_API int bgt_gpu_lattice_set_stream(bgt_gpu_lattice *lattice, void *stream);
@@ -160,6 +165,15 @@ BGT_GPU_API int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int 
 									double threshold_up, double threshold_lo, uint64_t seed, uint64_t session,
 									uint32_t true_state, uint32_t *experiments, uint32_t *responses,
 									uint32_t *positive_masks, uint32_t *negative_masks);
+
+/* Kernel timing for benchmarks: while enabled, every launch of the two
+ * lattice passes is bracketed by CUDA events on its stream.
+ * bgt_gpu_profile_read synchronises and reports, per pass (index 0: the
+ * update + low-bit zeta pass, 1: the high-bit zeta + selection pass), the
+ * number of launches and their summed device milliseconds since the last
+ * read, then resets the counters. */
+BGT_GPU_API int bgt_gpu_profile_enable(int enable);
+BGT_GPU_API int bgt_gpu_profile_read(uint64_t *launches, double *milliseconds);
 
 /* Thread-local description of the last failure ("" when none). */
 BGT_GPU_API const char *bgt_gpu_last_error(void);

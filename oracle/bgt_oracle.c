@@ -850,3 +850,28 @@ ORC_EXPORT int orc_run_simulation(int dilution, int subjects, int variants, cons
 	free(t.nodes);
 	return 0;
 }
+
+/* ------------------------------------------------------------ workload RNG */
+
+/* The seeded workload streams of include/bgt_session_rng.h, exported so the
+ * tests can pin host-side copies of them. */
+ORC_EXPORT double orc_uniform(uint64_t seed, uint64_t session, uint32_t tag, uint32_t index)
+{
+	return bgt_uniform(seed, session, tag, index);
+}
+
+ORC_EXPORT uint32_t orc_sample_truth(int atoms, const double *pi0, uint64_t seed, uint64_t session)
+{
+	return bgt_session_sample_truth(atoms, pi0, seed, session);
+}
+
+ORC_EXPORT void orc_sample_prior(int atoms, double lo, double hi, uint64_t seed, uint64_t session, double *pi0)
+{
+	bgt_session_sample_prior(atoms, lo, hi, seed, session, pi0);
+}
+
+ORC_EXPORT uint32_t orc_sample_response(int dilution, int subjects, int variants, uint32_t e, uint32_t s, double alpha,
+										double h, uint64_t seed, uint64_t session, uint32_t stage)
+{
+	return bgt_session_sample_response(dilution, subjects, variants, e, s, alpha, h, seed, session, stage);
+}

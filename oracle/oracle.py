@@ -102,6 +102,14 @@ class Oracle:
         L.orc_run_simulation.argtypes = [c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_int,
                                          c_double, c_double, _dp]
         L.orc_run_simulation.restype = c_int
+        L.orc_uniform.argtypes = [c_uint64, c_uint64, c_uint32, c_uint32]
+        L.orc_uniform.restype = c_double
+        L.orc_sample_truth.argtypes = [c_int, _dp, c_uint64, c_uint64]
+        L.orc_sample_truth.restype = c_uint32
+        L.orc_sample_prior.argtypes = [c_int, c_double, c_double, c_uint64, c_uint64, _dp]
+        L.orc_sample_response.argtypes = [c_int, c_int, c_int, c_uint32, c_uint32, c_double, c_double, c_uint64,
+                                          c_uint64, c_uint32]
+        L.orc_sample_response.restype = c_uint32
 
     # model -----------------------------------------------------------------
     def dilution_table(self, n, alpha=0.99, h=0.005):
@@ -172,6 +180,16 @@ class Oracle:
         post = np.ascontiguousarray(post, dtype=np.float64)
         scratch = np.empty((1 << n) * (1 << k))
         return int(self.lib.orc_select(_ptr(post), n, k, selector, _ptr(scratch)))
+
+    # workload streams --------------------------------------------------------
+    def sample_prior(self, atoms, lo, hi, seed, session):
+        out = np.empty(atoms)
+        self.lib.orc_sample_prior(atoms, lo, hi, seed, session, _ptr(out))
+        return out
+
+    def sample_truth(self, pi0, seed, session):
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        return int(self.lib.orc_sample_truth(len(pi0), _ptr(pi0), seed, session))
 
     # drivers ---------------------------------------------------------------
     def session(self, dilution, n, k, pi0, stages, seed, session, true_state, selector=AUTO, alpha=0.99,

@@ -1,0 +1,90 @@
+"""Generates tests/golden/reference_vectors.json from the reference library
+itself: its CPU provider compiled unmodified from its sources into
+oracle/_ref by oracle/ref/Makefile (strict IEEE build, plus the default
+-O3 -march=native -ffast-math build for the tree statistics).
+
+Run where the reference sources are present:
+
+    python -c "from oracle.oracle import build_reference; build_reference('/root/reference')"
+    python tests/golden/make_golden.py
+
+Every case is seeded; the JSON holds inputs and the reference's outputs.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle.oracle import Reference  # noqa: E402
+
+
+def main():
+    ref = Reference(strict=True)
+    fast = Reference(strict=False)
+    rng = np.random.default_rng(20261203)
+    out = {"generator": "tests/golden/make_golden.py", "source": "reference CPU provider (oracle/_ref)",
+           "model": [], "tree": [], "session": []}
+    # Model cases: prior, both update variants, selections, masses, classification.
+    for case in range(24):
+        k = [1, 1, 1, 2, 3, 1][case % 6]
+        n = {1: int(rng.integers(1, 9)), 2: int(rng.integers(1, 5)), 3: int(rng.integers(1, 4))}[k]
+        pi0 = rng.uniform(0.01, 0.3, n * k)
+        dilution = case % 2
+        e = int(rng.integers(1, 1 << n))
+        r = int(rng.integers(0, 1 << k))
+        prior = ref.prior(pi0, k)
+        upd = ref.update(dilution, n, k, prior, e, r, 0.99, 0.005, in_place=True)
+        upd_mul = ref.update(dilution, n, k, prior, e, r, 0.99, 0.005, in_place=False)
+        sel = {str(s): ref.select(upd, n, k, s) for s in ((0, 1, 2) if k == 1 else (0, 2))}
+        masses = ref.atom_masses(upd, n, k)
+        pos, neg = ref.classify(upd, n, k, 0.2, 0.2)
+        out["model"].append(dict(n=n, k=k, dilution=dilution, pi0=pi0.tolist(), e=e, r=r, prior=prior.tolist(),
+                                 update_divide=upd.tolist(), update_multiply=upd_mul.tolist(), select=sel,
+                                 atom_masses=masses.tolist(), classify_up=0.2, classify_lo=0.2, pos=pos, neg=neg))
+    # Trees: the reference's own CUDA-parity and regression cases plus seeded ones.
+    trees = [
+        (0, 1, 1, [0.2], 1, 0.01, 0.01, 0.0, 0),
+        (0, 2, 1, [0.2, 0.4], 1, 0.01, 0.01, 0.0, 0),
+        (1, 2, 1, [0.2, 0.4], 1, 0.01, 0.01, 0.0, 0),
+        (0, 1, 2, [0.2, 0.4], 1, 0.01, 0.01, 0.0, 0),
+        (0, 3, 1, [0.02, 0.05, 0.1], 3, 0.01, 0.01, 0.001, 1),
+        (0, 3, 1, [0.02, 0.05, 0.1], 3, 0.01, 0.01, 0.001, 2),
+        (1, 3, 1, [0.02, 0.05, 0.1], 3, 0.01, 0.01, 0.001, 1),
+        (1, 3, 1, [0.02, 0.05, 0.1], 3, 0.01, 0.01, 0.001, 2),
+        (0, 2, 2, [0.02, 0.04, 0.06, 0.08], 2, 0.01, 0.01, 0.001, 2),
+        (0, 2, 1, [0.2, 0.7], 2, 0.1, 0.1, 0.0, 0),
+        (1, 2, 1, [0.2, 0.7], 2, 0.1, 0.1, 0.0, 0),
+        (0, 2, 2, [0.2, 0.7, 0.4, 0.6], 2, 0.1, 0.1, 0.0, 0),
+        (0, 6, 2, [0.02] * 12, 6, 0.01, 0.01, 0.001, 0),
+    ]
+    for n in (8, 10, 12):
+        trees.append((n % 2, n, 1, rng.uniform(0.01, 0.2, n).tolist(), 4, 0.01, 0.01, 0.0, 0))
+    for (dil, n, k, pi0, depth, up, lo, br, sel) in trees:
+        stats = ref.run_simulation(dil, n, k, pi0, depth, up, lo, br, sel)
+        stats_fast = fast.run_simulation(dil, n, k, pi0, depth, up, lo, br, sel)
+        out["tree"].append(dict(dilution=dil, n=n, k=k, pi0=list(pi0), depth=depth, up=up, lo=lo, branch=br,
+                                selector=sel, stats=stats.tolist(), stats_default_build=stats_fast.tolist()))
+    # Sessions (bgt::Lattice call order, responses from the seeded streams).
+    for (dil, n, alpha, sel) in ((1, 10, 0.01, 2), (1, 12, 0.99, 2), (0, 11, 0.99, 1), (0, 9, 0.99, 0)):
+        pi0 = rng.uniform(0.005, 0.10, n)
+        truth = int(rng.integers(0, 1 << n))
+        res = ref.session(dil, n, 1, pi0, 8, 77, 5, truth, selector=sel, alpha=alpha, h=0.005)
+        out["session"].append(dict(dilution=dil, n=n, alpha=alpha, h=0.005, selector=sel, pi0=pi0.tolist(),
+                                   truth=truth, stages=8, seed=77, session=5,
+                                   experiments=res["experiments"].tolist(), responses=res["responses"].tolist(),
+                                   pos=res["pos"].tolist(), neg=res["neg"].tolist(),
+                                   posterior_sum=float(np.sum(res["posterior"])),
+                                   posterior_head=res["posterior"][:16].tolist()))
+    path = os.path.join(HERE, "reference_vectors.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=0)
+    print(path)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+"""The CPU oracle (oracle/bgt_oracle.c) pinned against the reference:
+its own known-answer tests, golden vectors generated by the reference library
+(tests/golden/make_golden.py) and, where the reference library is built in
+oracle/_ref, randomized bit-exact cross-checks."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle.oracle import Reference, reference_available
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = json.load(open(os.path.join(HERE, "golden", "reference_vectors.json")))
+
+
+def test_known_answers_model(oracle):
+    # tests/cpp/unit/model_math_test.cpp:41-62 (internal order).
+    np.testing.assert_allclose(oracle.prior([0.2, 0.4]), [0.08, 0.32, 0.12, 0.48], atol=1e-12)
+    post = oracle.update(0, 2, 1, oracle.prior([0.2, 0.4]), 1, 1, in_place=False)
+    den = 0.08 * 0.01 + 0.32 * 0.99 + 0.12 * 0.01 + 0.48 * 0.99
+    np.testing.assert_allclose(post, np.array([0.08 * 0.01, 0.32 * 0.99, 0.12 * 0.01, 0.48 * 0.99]) / den, atol=1e-12)
+    dil = oracle.dilution_table(2, 0.99, 0.005)
+    assert abs(dil[0, 0] - 0.99) < 1e-12 and abs(dil[0, 1] - 0.01) < 1e-12
+    assert abs(dil[1, 0] - 0.99) < 1e-12 and abs(dil[1, 1] - (1.0 - 0.99 / 1.005)) < 1e-12
+    assert abs(dil[1, 2] - 0.01) < 1e-12
+    # tests/cpp/unit/dilution_test.cpp:11-13 (public order == internal for a full pool).
+    assert abs(oracle.response_prob(1, 2, 1, 3, 1, 3) - 0.99) < 1e-12
+    assert abs(oracle.response_prob(1, 2, 1, 3, 1, 2) - (1.0 - 0.99 / 1.005)) < 1e-12
+    assert abs(oracle.response_prob(1, 2, 1, 3, 0, 2) - 0.99 / 1.005) < 1e-12
+
+
+def test_known_answers_selection(oracle):
+    # tests/cpp/unit/lattice_api_test.cpp:63-91; public state p is internal reverse(p).
+    post = oracle.prior([0.2, 0.4])
+    rev = {0: 0, 1: 2, 2: 1, 3: 3}
+    for e_pub, m in ((1, 0.60), (2, 0.80), (3, 0.48)):
+        assert abs(oracle.upset_mass(post, 2, rev[e_pub]) - m) < 1e-12
+    for sel in (0, 1, 2):
+        assert oracle.select(post, 2, 1, sel) == 3
+    post = oracle.update(0, 2, 1, post, rev[1], 1)
+    pos, neg = oracle.classify(post, 2, 0.01, 0.01)
+    assert pos == 0 and neg == rev[1]
+
+
+def test_known_answer_single_subject_tree(oracle):
+    # tests/cpp/support/assertions.hpp:80-92.
+    got = oracle.run_simulation(0, 1, 1, [0.2], 1)
+    np.testing.assert_allclose(got, [2, 0.792, 0.002, 0.0, 0.002, 0.206, 1.0, 1.0], atol=1e-12)
+
+
+@pytest.mark.parametrize("case", range(len(GOLDEN["model"])))
+def test_golden_model(oracle, case):
+    c = GOLDEN["model"][case]
+    n, k, dil = c["n"], c["k"], c["dilution"]
+    prior = oracle.prior(c["pi0"])
+    np.testing.assert_array_equal(prior, c["prior"])
+    np.testing.assert_array_equal(oracle.update(dil, n, k, prior, c["e"], c["r"], in_place=True), c["update_divide"])
+    np.testing.assert_array_equal(oracle.update(dil, n, k, prior, c["e"], c["r"], in_place=False),
+                                  c["update_multiply"])
+    post = np.array(c["update_divide"])
+    for sel, want in c["select"].items():
+        assert oracle.select(post, n, k, int(sel)) == want
+    np.testing.assert_array_equal(oracle.atom_masses(post, n * k), c["atom_masses"])
+    assert oracle.classify(post, n * k, c["classify_up"], c["classify_lo"]) == (c["pos"], c["neg"])
+
+
+@pytest.mark.parametrize("case", range(len(GOLDEN["tree"])))
+def test_golden_tree(oracle, case):
+    c = GOLDEN["tree"][case]
+    got = oracle.run_simulation(c["dilution"], c["n"], c["k"], c["pi0"], c["depth"], c["up"], c["lo"], c["branch"],
+                                c["selector"])
+    np.testing.assert_array_equal(got, c["stats"])
+    # The reference's default build (-ffast-math) agrees within the reference's own tolerance.
+    np.testing.assert_allclose(got, c["stats_default_build"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", range(len(GOLDEN["session"])))
+def test_golden_session(oracle, case):
+    c = GOLDEN["session"][case]
+    got = oracle.session(c["dilution"], c["n"], 1, c["pi0"], c["stages"], c["seed"], c["session"], c["truth"],
+                         selector=c["selector"], alpha=c["alpha"], h=c["h"])
+    for key in ("experiments", "responses", "pos", "neg"):
+        np.testing.assert_array_equal(got[key], c[key])
+    np.testing.assert_array_equal(got["posterior"][:16], c["posterior_head"])
+    assert float(np.sum(got["posterior"])) == c["posterior_sum"]
+
+
+def test_workload_streams_match_host_copies(oracle):
+    import bench
+
+    for session in (0, 1, 7, (3 << 32) + 5):
+        pi0 = oracle.sample_prior(24, bench.PRIOR_LO, bench.PRIOR_HI, bench.SEED, session)
+        np.testing.assert_array_equal(pi0, bench.session_prior(bench.SEED, session))
+        assert oracle.sample_truth(pi0, bench.SEED, session) == bench.session_truth(bench.SEED, session, pi0)
+
+
+@pytest.mark.reference
+@pytest.mark.skipif(not reference_available(), reason="reference library not built here (oracle/_ref)")
+def test_randomized_bit_exact_against_reference(oracle):
+    ref = Reference(strict=True)
+    rng = np.random.default_rng(99)
+    for trial in range(30):
+        k = [1, 1, 2, 3][trial % 4]
+        n = {1: int(rng.integers(1, 12)), 2: int(rng.integers(1, 6)), 3: int(rng.integers(1, 4))}[k]
+        pi0 = rng.uniform(0.005, 0.3, n * k)
+        dil = trial % 2
+        post = oracle.prior(pi0)
+        np.testing.assert_array_equal(post, ref.prior(pi0, k))
+        for _ in range(3):
+            e = int(rng.integers(1, 1 << n))
+            r = int(rng.integers(0, 1 << k))
+            nxt = oracle.update(dil, n, k, post, e, r)
+            np.testing.assert_array_equal(nxt, ref.update(dil, n, k, post, e, r))
+            post = nxt
+        for sel in ((0, 1, 2) if k == 1 else (0, 2)):
+            assert oracle.select(post, n, k, sel) == ref.select(post, n, k, sel)
+    for (dil, n, depth) in ((0, 7, 5), (1, 8, 4), (0, 9, 3)):
+        pi0 = rng.uniform(0.01, 0.2, n)
+        np.testing.assert_array_equal(oracle.run_simulation(dil, n, 1, pi0, depth),
+                                      ref.run_simulation(dil, n, 1, pi0, depth))
