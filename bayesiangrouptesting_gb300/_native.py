@@ -55,6 +55,7 @@ SIGNATURES = {
     "bgt_gpu_lattice_reset": ([c_void_p, _dp], c_int),
     "bgt_gpu_profile_enable": ([c_int], c_int),
     "bgt_gpu_profile_read": ([POINTER(c_uint64), _dp], c_int),
+    "bgt_gpu_select_noalloc": ([c_void_p, c_int, c_int, c_void_p, c_void_p], c_int),
     "bgt_gpu_last_error": ([], c_char_p),
     "bgt_gpu_kernel_launch_count": ([], c_uint64),
 }

@@ -1,0 +1,226 @@
+// Allocation-free experiment selection.
+//
+// Some callers cannot call cudaMalloc: code running inside a CUDA stream
+// capture that must not create allocations the graph does not own, processes
+// whose device memory is entirely handed out by another allocator (a serving
+// framework's arena), and real-time loops that must not take the driver's
+// allocation locks.  bgt_gpu_select_noalloc serves them: it selects the
+// Op-BHA / Op-BBPA experiment of a caller-owned device posterior using only
+// the fixed scratch below, which lives in this library's static device
+// memory, so the call itself allocates nothing.
+//
+// The scratch holds the two selection passes' working state for lattices of
+// up to kNoAllocMaxSubjects binary subjects (2^20 states): the zeta partial
+// sums (8 MB), the per-tile totals and scales, the per-block winners and the
+// pass state.  Every GPU that loads the library keeps this array until the
+// process exits.  All calls share it and it keeps the last call's contents;
+// the set-up kernel of each call clears what must start at zero (counters,
+// error flag), and everything else is overwritten before it is read.  Calls
+// whose work overlaps on the GPU (on different streams, or on one device from
+// several threads without ordering) race on the shared scratch.
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "bgt_gpu.h"
+#include "lattice_kernels.cuh"
+#include "provider_internal.h"
+
+namespace bgt_gpu
+{
+
+__global__ void k1_zeta_low(LatticeDev *states, int count, int per);
+__global__ void k2_zeta_high_select(LatticeDev *states, int count, int per);
+
+namespace
+{
+
+constexpr int kNoAllocMaxSubjects = 20;
+constexpr int kNoAllocMaxStates = 1 << kNoAllocMaxSubjects;
+constexpr int kNoAllocMaxTiles = kNoAllocMaxStates >> kTileBits;
+constexpr int kNoAllocMaxBlocks = kTileElems / kMinColW;
+
+// The static scratch.  Host code must not use these names as addresses: on
+// the host they are stand-ins, and a kernel handed one would fault or, where
+// the GPU can reach host memory, silently use the wrong memory.  The device
+// address comes from cudaGetSymbolAddress at set-up.
+// Every member starts on a 256-byte boundary, as a cudaMalloc'd buffer would:
+// the partial sums are written with 32-byte vector stores and read with bulk
+// copies, which need 32- and 16-byte alignment.
+struct NoAllocScratch
+{
+	LatticeDev state; // first member: the passes take its address as their state
+	alignas(256) unsigned long long m1[kNoAllocMaxStates];
+	alignas(256) unsigned long long tile_total[kNoAllocMaxTiles];
+	alignas(256) int tile_scale[kNoAllocMaxTiles];
+	alignas(256) unsigned long long blk_score[kNoAllocMaxBlocks];
+	alignas(256) unsigned int blk_e[kNoAllocMaxBlocks];
+};
+static_assert(offsetof(NoAllocScratch, state) == 0, "pass state first");
+static_assert(offsetof(NoAllocScratch, m1) % 256 == 0, "partial sums 256-byte aligned");
+static_assert(offsetof(NoAllocScratch, tile_total) % 256 == 0, "tile totals aligned");
+static_assert(offsetof(NoAllocScratch, tile_scale) % 256 == 0, "tile scales aligned");
+static_assert(offsetof(NoAllocScratch, blk_score) % 256 == 0, "block scores aligned");
+static_assert(offsetof(NoAllocScratch, blk_e) % 256 == 0, "block winners aligned");
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+constexpr int kMaxDevices = 64;
+NoAllocScratch *g_scratch_addr[kMaxDevices] = {};
+
+// Fills the pass state for a load-only selection of `posterior` (device code
+// names the scratch directly).
+__global__ void noalloc_setup(const double *posterior, LatticeGeometry g)
+{
+	if (threadIdx.x != 0 || blockIdx.x != 0)
+		return;
+	NoAllocScratch &s = g_noalloc_scratch;
+	LatticeDev &L = s.state;
+	L.n = g.n;
+	L.k = 1;
+	L.atoms = g.atoms;
+	L.tbits = g.tbits;
+	L.hbits = g.hbits;
+	L.nblk = g.nblk;
+	L.colw = g.colw;
+	L.logw = g.logw;
+	L.dilution = 0;
+	L.orig_n = g.n;
+	L.q_in = posterior;
+	L.q_out = nullptr;
+	L.m1 = s.m1;
+	L.tile_total = s.tile_total;
+	L.tile_scale = s.tile_scale;
+	L.blk_score = s.blk_score;
+	L.blk_e = s.blk_e;
+	L.dil = nullptr;
+	L.prior_lo = nullptr;
+	L.prior_hi = nullptr;
+	L.mode = kLoad;
+	L.pend_e = 0;
+	L.pend_r = 0;
+	L.z_norm = 1.0;
+	L.active = g.n >= 32 ? 0xFFFFFFFFu : ((1u << g.n) - 1u);
+	L.pos = 0;
+	L.neg = 0;
+	L.classify_on_update = 0;
+	L.masses_in_k2 = 0;
+	L.skip = 0;
+	L.error = 0;
+	L.k1_count = 0;
+	L.k2_count = 0;
+	L.sess_active = 0;
+}
+
+// Writes the selection (or 0xFFFFFFFF after a device-detected error).
+__global__ void noalloc_finish(uint32_t *experiment)
+{
+	if (threadIdx.x == 0 && blockIdx.x == 0)
+	{
+		const LatticeDev &L = g_noalloc_scratch.state;
+		*experiment = L.error ? 0xFFFFFFFFu : L.best_e;
+	}
+}
+
+// Once per device, with that device current: the scratch's device address
+// and the passes' shared-memory attributes.
+int noalloc_setup_device(NoAllocScratch **out)
+{
+	int dev = 0;
+	cudaError_t err = cudaGetDevice(&dev);
+	if (err != cudaSuccess)
+	{
+		set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(err));
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+	if (dev < 0 || dev >= kMaxDevices)
+	{
+		set_error("device index beyond the allocation-free entry point's device table");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (g_scratch_addr[dev] == nullptr)
+	{
+		void *ptr = nullptr;
+		err = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+		if (err != cudaSuccess)
+		{
+			set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(err));
+			return BGT_GPU_RUNTIME_FAILURE;
+		}
+		try
+		{
+			configure_kernels();
+		}
+		catch (const std::exception &ex)
+		{
+			set_error(ex.what());
+			return BGT_GPU_RUNTIME_FAILURE;
+		}
+		g_scratch_addr[dev] = static_cast<NoAllocScratch *>(ptr);
+	}
+	*out = g_scratch_addr[dev];
+	return BGT_GPU_OK;
+}
+
+} // namespace
+} // namespace bgt_gpu
+
+using namespace bgt_gpu;
+
+extern "C" int bgt_gpu_select_noalloc(const double *posterior, int subjects, int selector, uint32_t *experiment,
+									  void *stream)
+{
+	if (posterior == nullptr || experiment == nullptr)
+	{
+		set_error("null posterior or experiment pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (subjects < 1 || subjects > kNoAllocMaxSubjects)
+	{
+		set_error("bgt_gpu_select_noalloc handles 1 to 20 binary subjects (2^20 states of static scratch); "
+				  "larger lattices need bgt_gpu_lattice_create");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (selector != 0 && selector != 1 && selector != 2)
+	{
+		set_error("unsupported selector");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (reinterpret_cast<uintptr_t>(posterior) % 16 != 0)
+	{
+		set_error("the posterior must be 16-byte aligned (it is read with bulk copies)");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	NoAllocScratch *scratch = nullptr;
+	const int rc = noalloc_setup_device(&scratch);
+	if (rc != BGT_GPU_OK)
+		return rc;
+	try
+	{
+		const cudaStream_t s = static_cast<cudaStream_t>(stream);
+		const LatticeGeometry g = make_geometry(subjects, 1);
+		noalloc_setup<<<1, 32, 0, s>>>(posterior, g);
+		cuda_check(cudaGetLastError(), "noalloc setup launch");
+		count_launches(1);
+		// The pass state is the scratch's first member.
+		LatticeDev *state = reinterpret_cast<LatticeDev *>(scratch);
+		const int sms = sm_count();
+		const int per1 = 1 << g.hbits;
+		k1_zeta_low<<<per1 < sms ? per1 : sms, kThreads, k1_smem_bytes(), s>>>(state, 1, per1);
+		cuda_check(cudaGetLastError(), "noalloc k1 launch");
+		k2_zeta_high_select<<<g.nblk < sms ? g.nblk : sms, kThreads, k2_smem_bytes(g.hbits), s>>>(state, 1, g.nblk);
+		cuda_check(cudaGetLastError(), "noalloc k2 launch");
+		count_launches(2);
+		noalloc_finish<<<1, 32, 0, s>>>(experiment);
+		cuda_check(cudaGetLastError(), "noalloc finish launch");
+		count_launches(1);
+	}
+	catch (const std::exception &ex)
+	{
+		set_error(ex.what());
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+	return BGT_GPU_OK;
+}

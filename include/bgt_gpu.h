@@ -175,6 +175,29 @@ BGT_GPU_API int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int 
 BGT_GPU_API int bgt_gpu_profile_enable(int enable);
 BGT_GPU_API int bgt_gpu_profile_read(uint64_t *launches, double *milliseconds);
 
+/* Allocation-free selection, for callers that cannot allocate device memory
+ * (inside a stream capture that must not create allocations, in processes
+ * whose device memory belongs to another allocator, or in loops that must not
+ * take the driver's allocation locks).  No counterpart in the reference.
+ *
+ * Selects the Op-BHA / Op-BBPA experiment (selector 0, 1 or 2; for binary
+ * lattices all three give the same experiment) of a caller-owned device
+ * posterior of 2^subjects FP64 values in internal state order (16-byte
+ * aligned), any normalisation, and writes it (internal bit order) to the device word
+ * `experiment`, or 0xFFFFFFFF when the device detected an error.  Work is
+ * enqueued on `stream` (a cudaStream_t; 0 = default stream) and the call
+ * returns without synchronising.
+ *
+ * Scratch is a fixed static device array sized for at most 20 subjects
+ * (2^20 states); larger requests return status 2 with a message.  The call
+ * makes no cudaMalloc, cudaFree or other allocating call.  The first call on
+ * each device looks up the scratch's device address and sets the kernels'
+ * shared-memory attributes; make that first call before any stream capture.
+ * All calls share the scratch, so calls whose work overlaps on the GPU race;
+ * order them on one stream. */
+BGT_GPU_API int bgt_gpu_select_noalloc(const double *posterior, int subjects, int selector, uint32_t *experiment,
+									   void *stream);
+
 /* Thread-local description of the last failure ("" when none). */
 BGT_GPU_API const char *bgt_gpu_last_error(void);
 
