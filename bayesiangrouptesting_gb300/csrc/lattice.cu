@@ -171,7 +171,7 @@ LatticeGeometry make_geometry(int n, int k)
 }
 
 // Validates a request against what this build supports; returns 0 or a status.
-int check_supported(int subjects, int variants, std::string *why)
+int check_supported(int subjects, int variants, int dilution, std::string *why)
 {
 	if (subjects <= 0 || variants <= 0)
 	{
@@ -183,15 +183,23 @@ int check_supported(int subjects, int variants, std::string *why)
 		*why = "subjects * variants exceeds 30 atoms";
 		return BGT_GPU_UNSUPPORTED;
 	}
-	if (variants != 1)
+	if (subjects * variants > kTileBits + kMaxHighBits)
 	{
-		*why = "multinomial (variants > 1) lattices are not supported by this build";
+		*why = "lattices above 24 atoms (subjects * variants) are not supported by this build";
 		return BGT_GPU_UNSUPPORTED;
 	}
-	if (subjects > kTileBits + kMaxHighBits)
+	if (variants > 1)
 	{
-		*why = "binary lattices above 24 subjects are not supported by this build";
-		return BGT_GPU_UNSUPPORTED;
+		long long entries = 1;
+		for (int v = 0; v < variants; v++)
+		{
+			entries *= dilution ? subjects + 1 : 2;
+			if (entries > kMaxClassTable)
+			{
+				*why = "too many multinomial likelihood classes for this build";
+				return BGT_GPU_UNSUPPORTED;
+			}
+		}
 	}
 	return 0;
 }
@@ -229,6 +237,7 @@ struct bgt_gpu_lattice
 	double *dil = nullptr;
 	double *prior_lo = nullptr, *prior_hi = nullptr, *pi0 = nullptr;
 	unsigned long long *scratch_u64 = nullptr;
+	unsigned long long *ftab = nullptr; // k >= 2 feature masses
 	unsigned int *sess_out = nullptr; // 4 * max stages
 	int sess_capacity = 0;
 	bool have_dilution = false;
@@ -252,6 +261,7 @@ struct bgt_gpu_lattice
 		cudaFree(prior_hi);
 		cudaFree(pi0);
 		cudaFree(scratch_u64);
+		cudaFree(ftab);
 		cudaFree(sess_out);
 		if (own_stream)
 			cudaStreamDestroy(own_stream);
@@ -395,7 +405,7 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 	}
 	*out = nullptr;
 	std::string why;
-	if (const int rc = check_supported(subjects, variants, &why))
+	if (const int rc = check_supported(subjects, variants, lattice_type, &why))
 	{
 		set_error(why);
 		return rc;
@@ -442,6 +452,9 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			cuda_check(cudaMalloc(&lat->prior_hi, rows * sizeof(double)), "alloc prior hi");
 			cuda_check(cudaMalloc(&lat->pi0, g.atoms * sizeof(double)), "alloc pi0");
 			cuda_check(cudaMalloc(&lat->scratch_u64, 64 * sizeof(unsigned long long)), "alloc scratch");
+			if (variants > 1)
+				cuda_check(cudaMalloc(&lat->ftab, (size_t{1} << (subjects + variants)) * sizeof(unsigned long long)),
+						   "alloc feature masses");
 			cuda_check(cudaMemcpyAsync(lat->pi0, prior, g.atoms * sizeof(double), cudaMemcpyHostToDevice, lat->stream),
 					   "prior upload");
 			const unsigned int span = std::max<unsigned int>(1u << g.tbits, static_cast<unsigned int>(rows));
@@ -472,6 +485,7 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			h.dil = lat->dil;
 			h.prior_lo = lat->prior_lo;
 			h.prior_hi = lat->prior_hi;
+			h.ftab = lat->ftab;
 			h.mode = kGenerate;
 			h.z_norm = 1.0;
 			h.active = g.n >= 32 ? 0xFFFFFFFFu : ((1u << g.n) - 1u);

@@ -146,7 +146,7 @@ __device__ __forceinline__ void argmin_block(u64 &s, unsigned int &e, u64 *ws, u
 struct LatCache
 {
 	int li;
-	int mode, tbits, hbits, colw, logw, dilution, skip, n;
+	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix;
 	unsigned int e, active;
 	const double *q_in;
 	double *q_out;
@@ -158,6 +158,7 @@ struct LatCache
 	int masses;
 	u64 *tile_total;
 	int *tile_scale;
+	u64 *ftab;
 };
 
 struct PipeShared
@@ -167,6 +168,7 @@ struct PipeShared
 	double ctab[kMaxClasses];
 	float fred[32];
 	u64 ws[32];
+	u64 wsh[32];
 	unsigned int we[32];
 	double dred[32];
 	u64 ured[32];
@@ -183,6 +185,10 @@ struct PipeShared
 extern __shared__ __align__(1024) unsigned char g_smem[];
 __shared__ PipeShared ps;
 __shared__ int g_shift[1 << kMaxHighBits];
+// Mixed-radix likelihood classes of a multinomial update: entry
+// sum_v c_v * radix^v holds prod_v f_v(c_v) / Z (variant order, as
+// response_prob multiplies them, src/core/model/replicated_lattice.cpp:8-28).
+__shared__ double g_ctab[kMaxClassTable];
 
 __device__ __forceinline__ double *tile_f64(int b) { return reinterpret_cast<double *>(g_smem + b * kSmemBuf); }
 __device__ __forceinline__ u64 *tile_u64(int b) { return reinterpret_cast<u64 *>(g_smem + b * kSmemBuf); }
@@ -307,7 +313,23 @@ struct ItemCfg
 	int tbits, hbits, colw, logw;
 	int dilution_classes; // 1: class = popcount(e & s); 0: class = contained
 	double c_in, c_out;   // non-dilution update factors (contained / not)
+	int k, n, radix;      // k >= 2: mixed-radix classes into g_ctab
 };
+
+// Mixed-radix likelihood class of state s for a multinomial update.
+__device__ __forceinline__ int multinomial_class(const ItemCfg &cfg, unsigned int s)
+{
+	const unsigned int mask = (1u << cfg.n) - 1u;
+	int idx = 0, w = 1;
+	for (int v = 0; v < cfg.k; v++)
+	{
+		const unsigned int sv = (s >> (v * cfg.n)) & mask;
+		const int c = cfg.dilution_classes ? __popc(cfg.e & sv) : ((cfg.e & sv) == cfg.e ? 1 : 0);
+		idx += c * w;
+		w *= cfg.radix;
+	}
+	return idx;
+}
 
 // One K1 work item (tile r of lattice L), specialised on the K1 mode.
 template <int kMode>
@@ -349,7 +371,12 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 			if (kMode == kUpdate)
 			{
 				const unsigned int s0 = static_cast<unsigned int>(base) | x;
-				if (cfg.dilution_classes)
+				if (cfg.k > 1)
+				{
+					p.x *= g_ctab[multinomial_class(cfg, s0)];
+					p.y *= g_ctab[multinomial_class(cfg, s0 | 1u)];
+				}
+				else if (cfg.dilution_classes)
 				{
 					p.x *= ps.ctab[__popc(e & s0)];
 					p.y *= ps.ctab[__popc(e & (s0 | 1u))];
@@ -454,16 +481,48 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 
 // Loads the per-lattice constants of lattice li into ps.lc (warp 0), the
 // likelihood-class table included for updates.
+// K1 only (the table lives in K1's shared memory): the multinomial class
+// table of lattice L's pending update, filled by all threads.
+__device__ __forceinline__ void load_class_table(const LatticeDev &L)
+{
+	const int k = L.k;
+	if (k < 2 || L.mode != kUpdate)
+		return;
+	const unsigned int e = L.pend_e;
+	const int pool = __popc(e);
+	const int radix = L.dilution ? pool + 1 : 2;
+	int entries = 1;
+	for (int v = 0; v < k; v++)
+		entries *= radix;
+	const double z = L.z_norm;
+	for (int idx = threadIdx.x; idx < entries && idx < kMaxClassTable; idx += kThreads)
+	{
+		double f = 1.0;
+		int rest = idx;
+		for (int v = 0; v < k; v++)
+		{
+			const int c = rest % radix;
+			rest /= radix;
+			// Non-dilution class c = contained (1) or not (0); dilution class = popcount(e & s_v).
+			const int pc = L.dilution ? c : (c ? pool : (pool > 0 ? pool - 1 : 0));
+			f *= binary_likelihood(L.dilution, pool, pc, (L.pend_r >> v) & 1u, L.dil, L.orig_n + 1);
+		}
+		g_ctab[idx] = f / z;
+	}
+}
+
 __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 {
 	const unsigned int tid = threadIdx.x;
+	const int mode = L.mode;
+	const unsigned int e = L.pend_e;
+	const int k = L.k;
+	const int pool = __popc(e);
+	const int radix = L.dilution ? pool + 1 : 2;
 	if (tid < 32)
 	{
-		const int mode = L.mode;
-		const unsigned int e = L.pend_e;
-		if (mode == kUpdate)
+		if (mode == kUpdate && k == 1)
 		{
-			const int pool = __popc(e);
 			ps.ctab[tid] = static_cast<int>(tid) <= pool
 							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1) / L.z_norm
 							   : 0.0;
@@ -482,6 +541,8 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.dilution = L.dilution;
 			c.skip = L.skip;
 			c.n = L.n;
+			c.k = k;
+			c.radix = radix;
 			c.active = L.active;
 			c.q_in = L.q_in;
 			c.q_out = L.q_out;
@@ -492,8 +553,9 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.masses = L.masses_in_k2;
 			c.tile_total = L.tile_total;
 			c.tile_scale = L.tile_scale;
-			c.c_in = mode == kUpdate ? ps.ctab[__popc(e)] : 0.0;
-			c.c_out = mode == kUpdate ? ps.ctab[0] : 0.0;
+			c.ftab = L.ftab;
+			c.c_in = mode == kUpdate && k == 1 ? ps.ctab[pool] : 0.0;
+			c.c_out = mode == kUpdate && k == 1 ? ps.ctab[0] : 0.0;
 		}
 	}
 }
@@ -517,6 +579,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 		ps.flag = 0;
 	}
 	load_lattice_cache(states[w / per], static_cast<int>(w / per));
+	load_class_table(states[w / per]);
 	__syncthreads();
 	// Thread 0 issues the bulk copy of item `item` into buffer b (no copy
 	// for generated priors); same-lattice items use the cached constants.
@@ -559,6 +622,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 		{
 			__syncthreads();
 			load_lattice_cache(states[li], li);
+			load_class_table(states[li]);
 			__syncthreads();
 		}
 		const int mode = ps.lc.mode;
@@ -603,6 +667,9 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 		cfg.dilution_classes = ps.lc.dilution;
 		cfg.c_in = ps.lc.c_in;
 		cfg.c_out = ps.lc.c_out;
+		cfg.k = ps.lc.k;
+		cfg.n = ps.lc.n;
+		cfg.radix = ps.lc.radix;
 		u64 tile_total = 0;
 		int tile_scale = 0;
 		bool abort;
@@ -659,26 +726,141 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 
 // ------------------------------------------------------------------ K2
 
-// K2 epilogue of lattice L: the block winners' argmin and, in session mode,
+typedef unsigned __int128 u128;
+
+__device__ __forceinline__ bool better128(u128 s, unsigned int e, u128 bs, unsigned int be)
+{
+	return s < bs || (s == bs && e < be);
+}
+
+// Block argmin over 128-bit scores (lowest index on ties); thread 0 holds it.
+__device__ __forceinline__ void argmin128_block(u128 &s, unsigned int &e)
+{
+	for (int o = 16; o > 0; o >>= 1)
+	{
+		const u64 lo = __shfl_xor_sync(0xFFFFFFFFu, static_cast<u64>(s), o);
+		const u64 hi = __shfl_xor_sync(0xFFFFFFFFu, static_cast<u64>(s >> 64), o);
+		const unsigned int oe = __shfl_xor_sync(0xFFFFFFFFu, e, o);
+		const u128 os = (static_cast<u128>(hi) << 64) | lo;
+		if (better128(os, oe, s, e))
+		{
+			s = os;
+			e = oe;
+		}
+	}
+	if ((threadIdx.x & 31) == 0)
+	{
+		ps.ws[threadIdx.x >> 5] = static_cast<u64>(s);
+		ps.wsh[threadIdx.x >> 5] = static_cast<u64>(s >> 64);
+		ps.we[threadIdx.x >> 5] = e;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		for (int w = 1; w < kThreads / 32; w++)
+		{
+			const u128 os = (static_cast<u128>(ps.wsh[w]) << 64) | ps.ws[w];
+			if (better128(os, ps.we[w], s, e))
+			{
+				s = os;
+				e = ps.we[w];
+			}
+		}
+	}
+}
+
+// Multinomial Op-BBPA of lattice L from its feature masses F_B(E) (whole CTA),
+// restating best_multinomial_partition_candidate (bbpa.cpp:416-460) in exact
+// integer arithmetic: bucket_R(E) = sum over X subset of R of
+// (-1)^|X| F_{~R | X}(E) (modular u64 arithmetic, exact because every bucket
+// is a non-negative mass below 2^63), score(E) = sum_R |2^k bucket_R(E) - Z|,
+// the same ordering as sum_R |bucket_R / Z - 1/2^k|.  Candidates are the
+// subsets of the active subjects; the lowest index wins ties.  Also writes
+// the atom masses F_{v}({j}) when the lattice keeps them here.  Returns the
+// winner (valid in thread 0).
+__device__ unsigned int multinomial_select(LatticeDev &L)
+{
+	const int n = L.n, k = L.k;
+	const unsigned int e_count = 1u << n;
+	const int responses = 1 << k;
+	const int all = responses - 1;
+	const u64 zg = L.z_g;
+	const u64 *F = L.ftab;
+	const unsigned int active = L.active;
+	if (L.masses_in_k2)
+	{
+		for (int atom = threadIdx.x; atom < n * k; atom += kThreads)
+		{
+			const int v = atom / n, j = atom % n;
+			L.atom_fixed[atom] = __ldcg(F + ((static_cast<size_t>(1u << v) << n) | (1u << j)));
+		}
+	}
+	u128 best = ~static_cast<u128>(0);
+	unsigned int best_e = 0xFFFFFFFFu;
+	for (unsigned int E = threadIdx.x; E < e_count; E += kThreads)
+	{
+		if (E & ~active)
+			continue;
+		u128 score = 0;
+		for (int resp = 0; resp < responses; resp++)
+		{
+			const int positive = (~resp) & all;
+			u64 bucket = 0;
+			for (int extra = resp;; extra = (extra - 1) & resp)
+			{
+				const int fs = positive | extra;
+				const u64 feature = (fs == 0 || E == 0) ? zg : __ldcg(F + ((static_cast<size_t>(fs) << n) | E));
+				if ((__popc(static_cast<unsigned int>(extra)) & 1) == 0)
+					bucket += feature;
+				else
+					bucket -= feature;
+				if (extra == 0)
+					break;
+			}
+			const u128 d = static_cast<u128>(bucket) << k;
+			score += d > zg ? d - zg : static_cast<u128>(zg) - d;
+		}
+		if (score < best)
+		{
+			best = score;
+			best_e = E;
+		}
+	}
+	__syncthreads();
+	argmin128_block(best, best_e);
+	return best_e;
+}
+
+// K2 epilogue of lattice L: the winning experiment (the block winners' argmin
+// for k = 1, the multinomial scoring for k >= 2) and, in session mode,
 // classification, the drawn response and the queued update.
 __device__ void k2_epilogue(LatticeDev &L, int per)
 {
 	u64 bs = ~0ull;
 	unsigned int be = 0xFFFFFFFFu;
-	for (int i = threadIdx.x; i < per; i += kThreads)
+	if (L.k > 1)
 	{
-		const u64 s2 = __ldcg(L.blk_score + i);
-		const unsigned int e2 = __ldcg(L.blk_e + i);
-		if (better(s2, e2, bs, be))
-		{
-			bs = s2;
-			be = e2;
-		}
+		be = multinomial_select(L);
+		bs = 0;
 	}
-	__syncthreads();
-	argmin_block(bs, be, ps.ws, ps.we);
+	else
+	{
+		for (int i = threadIdx.x; i < per; i += kThreads)
+		{
+			const u64 s2 = __ldcg(L.blk_score + i);
+			const unsigned int e2 = __ldcg(L.blk_e + i);
+			if (better(s2, e2, bs, be))
+			{
+				bs = s2;
+				be = e2;
+			}
+		}
+		__syncthreads();
+		argmin_block(bs, be, ps.ws, ps.we);
+	}
 	if (threadIdx.x == 0)
 	{
+		__threadfence();
 		L.best_score = bs;
 		L.best_e = be;
 		if (L.sess_active)
@@ -870,7 +1052,38 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		const unsigned int y0 = map_c(tid, 0);
 		u64 best = ~0ull;
 		int best_j = -1;
-		if ((active & all) == all)
+		if (ps.lc.k > 1)
+		{
+			// Multinomial: keep the zeta values at the points sum_{v in B} E << (v n),
+			// which are the BBPA feature masses F_B(E) (bbpa.cpp:222-285); the
+			// lattice's last block scores them.
+			const int nn = ps.lc.n, kk = ps.lc.k;
+			const unsigned int nmask = (1u << nn) - 1u;
+			u64 *ftab = ps.lc.ftab;
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+			{
+				const unsigned int y = y0 + (j << 2);
+				if (y >= elems)
+					continue;
+				const unsigned int Eall = ((y >> logw) << tbits) | col_base | (y & wmask);
+				unsigned int ev = 0, bset = 0;
+				bool diag = true;
+				for (int v = 0; v < kk; v++)
+				{
+					const unsigned int c = (Eall >> (v * nn)) & nmask;
+					if (c)
+					{
+						diag &= ev == 0 || c == ev;
+						ev = c;
+						bset |= 1u << v;
+					}
+				}
+				if (diag && bset)
+					ftab[(static_cast<size_t>(bset) << nn) | ev] = a[j];
+			}
+		}
+		else if ((active & all) == all)
 		{
 #pragma unroll
 			for (int j = 0; j < kPerThread; j++)

@@ -56,6 +56,7 @@ constexpr int kMinColW = 4;                   // 32-byte row chunks at the least
 constexpr int kMaxHighBits = 11;              // K2 block = 2^h rows x W columns <= 2^13 values
 constexpr int kMaxAtoms = 30;
 constexpr int kMaxClasses = 32;               // likelihood classes for k = 1 (popcount 0..n)
+constexpr int kMaxClassTable = 4096;          // mixed-radix likelihood classes for k >= 2
 constexpr int kSmemBuf = kTileElems * 8;      // one 64 KB tile buffer
 constexpr int kPipeSmem = 3 * kSmemBuf;       // two bulk-copy buffers + one work buffer
 
@@ -91,6 +92,7 @@ struct LatticeDev
 	const double *dil;             // [orig_n][orig_n + 1]
 	const double *prior_lo;        // [2^tbits]
 	const double *prior_hi;        // [2^hbits]
+	unsigned long long *ftab;      // k >= 2: BBPA feature masses F_B(E), [2^k][2^n], global scale
 	// ---- dynamic (device-updated) ----
 	int mode;                      // K1Mode for the next K1
 	unsigned int pend_e, pend_r;   // pending update

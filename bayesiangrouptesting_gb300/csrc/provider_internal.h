@@ -29,7 +29,7 @@ void count_launches(uint64_t n);
 void cuda_check(cudaError_t err, const char *what);
 void configure_kernels();
 LatticeGeometry make_geometry(int n, int k);
-int check_supported(int subjects, int variants, std::string *why);
+int check_supported(int subjects, int variants, int dilution, std::string *why);
 void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
 void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
 size_t k1_smem_bytes();

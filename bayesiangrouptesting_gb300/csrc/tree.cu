@@ -199,6 +199,7 @@ struct Level
 	int *tile_scale = nullptr;
 	unsigned long long *blk_score = nullptr;
 	unsigned int *blk_e = nullptr;
+	unsigned long long *ftab = nullptr;
 	std::vector<LatticeDev> host;
 
 	void release()
@@ -210,6 +211,8 @@ struct Level
 		cudaFree(tile_scale);
 		cudaFree(blk_score);
 		cudaFree(blk_e);
+		cudaFree(ftab);
+		ftab = nullptr;
 		states = nullptr;
 		q = nullptr;
 		m1 = nullptr;
@@ -239,6 +242,9 @@ void allocate_level(Level &lv, const LatticeGeometry &g)
 	cuda_check(cudaMalloc(&lv.tile_scale, count * rows * sizeof(int)), "alloc tile scales");
 	cuda_check(cudaMalloc(&lv.blk_score, count * g.nblk * sizeof(unsigned long long)), "alloc block scores");
 	cuda_check(cudaMalloc(&lv.blk_e, count * g.nblk * sizeof(unsigned int)), "alloc block winners");
+	if (g.k > 1)
+		cuda_check(cudaMalloc(&lv.ftab, count * (size_t{1} << (g.n + g.k)) * sizeof(unsigned long long)),
+				   "alloc feature masses");
 	lv.host.assign(count, LatticeDev{});
 }
 
@@ -252,6 +258,7 @@ void bind_level_buffers(Level &lv, const LatticeGeometry &g, size_t i, LatticeDe
 	d.tile_scale = lv.tile_scale + i * rows;
 	d.blk_score = lv.blk_score + i * g.nblk;
 	d.blk_e = lv.blk_e + i * g.nblk;
+	d.ftab = lv.ftab ? lv.ftab + i * (size_t{1} << (g.n + g.k)) : nullptr;
 }
 
 void flatten_preorder(const std::vector<HostNode> &tree, int node, std::vector<SweepNode> &out, int atoms)
@@ -367,8 +374,17 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 			const bool classified = __builtin_popcount(d.pos | d.neg) == g.atoms;
 			hn.leaf = classified || hn.stage >= search_depth;
 			d.skip = hn.leaf ? 1 : 0;
-			// Candidates: subjects with an unclassified atom (for k = 1, the unclassified atoms).
-			d.active = ~(d.pos | d.neg) & subject_mask;
+			// Candidates: the subjects with an unclassified atom, the subjects the
+			// reference's shrunk lattice still holds (shrink_plan.cpp:31-54).
+			{
+				const unsigned int clas = d.pos | d.neg;
+				unsigned int act = 0;
+				for (int j = 0; j < subjects; j++)
+					for (int v = 0; v < variants; v++)
+						if (!(clas & (1u << (v * subjects + j))))
+							act |= 1u << j;
+				d.active = act & subject_mask;
+			}
 			any_internal |= !hn.leaf;
 		}
 		if (!any_internal)
@@ -433,6 +449,7 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 		next.tile_scale = nullptr;
 		next.blk_score = nullptr;
 		next.blk_e = nullptr;
+		next.ftab = nullptr;
 	}
 	prev.release();
 	cur.release();
@@ -521,7 +538,7 @@ int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const do
 		return BGT_GPU_MISSING_DILUTION;
 	}
 	std::string why;
-	if (const int rc = check_supported(subjects, variants, &why))
+	if (const int rc = check_supported(subjects, variants, use_dilution, &why))
 	{
 		set_error(why);
 		return rc;

@@ -32,3 +32,31 @@ def gpu(native_lib):
     if not native_lib.bgt_cuda_provider_available():
         pytest.fail("GPU test selected but no CUDA device is available")
     return native_lib
+
+
+def assert_posterior_close(got, want, updates):
+    """Posterior parity with the oracle.
+
+    The shape must agree to 1e-13: got / want is one constant up to the
+    per-value rounding of the updates (a few ulp per update).  The constant
+    itself may differ from 1 by the oracle's own summation error: the
+    reference normalises by a sequential FP64 sum of N terms
+    (src/core/model/lattice_base.cpp:230-244), whose rounding error is about
+    sqrt(N) * 2^-53 per update, while the device sums exactly.  The bound
+    used is 1e-12 + updates * 4 * sqrt(N) * 2^-53; the reference's own
+    tests use 1e-12 absolute (tests/cpp/support/assertions.hpp:14-19).
+    """
+    import numpy as np
+
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    assert got.shape == want.shape
+    nz = want > 1e-250
+    ratio = got[nz] / want[nz]
+    mid = float(np.median(ratio))
+    shape_err = float(np.max(np.abs(ratio - mid))) if ratio.size else 0.0
+    assert shape_err <= 1e-13 * max(1, updates), f"posterior shape differs: {shape_err:.3e}"
+    bound = 1e-12 + updates * 4.0 * np.sqrt(got.size) * 2.0 ** -53
+    assert abs(mid - 1.0) <= bound, f"normalisation differs by {abs(mid - 1.0):.3e} > {bound:.3e}"
+    # Values too small to compare by ratio agree absolutely.
+    assert float(np.max(np.abs(got[~nz] - want[~nz]), initial=0.0)) <= 1e-250

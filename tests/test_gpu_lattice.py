@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 import bayesiangrouptesting_gb300 as bgt
+from conftest import assert_posterior_close
 
 pytestmark = pytest.mark.gpu
 
@@ -70,7 +71,7 @@ def test_update_and_select_sequence(gpu, oracle, dilution):
             r = int(rng.integers(0, 2))
             post = oracle.update(1 if dilution else 0, n, 1, post, e, r, 0.99, 0.005, in_place=True)
             lat.update(bgt.reverse_bits(e, n), r, table)
-            np.testing.assert_allclose(lat.posterior(), post, rtol=RTOL, atol=1e-300)
+            assert_posterior_close(lat.posterior(), post, step + 1)
             masses = oracle.atom_masses(post, n)
             np.testing.assert_allclose(lat.atom_masses(), masses, rtol=1e-12, atol=1e-18)
 
@@ -89,7 +90,7 @@ def test_device_session_matches_oracle(gpu, oracle, dilution, alpha):
             np.testing.assert_array_equal(got["responses"], want["responses"])
             np.testing.assert_array_equal(got["pos"], want["pos"])
             np.testing.assert_array_equal(got["neg"], want["neg"])
-            np.testing.assert_allclose(lat.posterior(), want["posterior"], rtol=RTOL, atol=1e-300)
+            assert_posterior_close(lat.posterior(), want["posterior"], 8)
 
 
 def test_errors_are_loud(gpu):
@@ -100,3 +101,59 @@ def test_errors_are_loud(gpu):
         lat.update(1, 1, None)
     with pytest.raises(bgt.Error):
         bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 31, [0.1] * 31)
+
+
+def test_multinomial_reference_pin(gpu, oracle):
+    # tests/cpp/unit/lattice_api_test.cpp:94-99: exact-transform BBPA equals brute force.
+    prior = [0.11, 0.23, 0.31, 0.41, 0.17, 0.29]
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 3, prior, variants=2)
+    got = lat.select_experiment(bgt.SelectorType.op_bbpa)
+    post = oracle.prior(prior)
+    assert got == oracle.select(post, 3, 2, 2)
+    # brute force over experiments and response buckets (lattice_api_test.cpp:10-53)
+    best, best_e = 9.0, 0
+    for e in range(8):
+        mass = [0.0] * 4
+        for s in range(64):
+            r = sum((1 << v) for v in range(2) if (e & ~((s >> (3 * v)) & 7)) != 0)
+            mass[r] += post[s]
+        score = sum(abs(m - 0.25) for m in mass)
+        if score < best:
+            best, best_e = score, e
+    assert got == best_e
+    with pytest.raises(bgt.Error):
+        lat.select_experiment(bgt.SelectorType.op_bha)
+
+
+@pytest.mark.parametrize("k,n,dilution", [(2, 3, False), (2, 6, True), (2, 9, False), (2, 12, True), (3, 4, False),
+                                          (3, 6, True), (3, 8, False), (4, 5, False)])
+def test_multinomial_session_matches_oracle(gpu, oracle, k, n, dilution):
+    rng = np.random.default_rng(1000 + 10 * k + n)
+    pi0 = rng.uniform(0.01, 0.12, n * k)
+    truth = int(rng.integers(0, 1 << (n * k)))
+    t = bgt.LatticeType.replicated_dilution if dilution else bgt.LatticeType.replicated_non_dilution
+    lat = bgt.Lattice(t, n, pi0, variants=k)
+    got = lat.run_session(6, truth, seed=3, session=9, selector=bgt.SelectorType.op_bbpa, alpha=0.99)
+    want = oracle.session(1 if dilution else 0, n, k, pi0, 6, 3, 9, truth, selector=2, alpha=0.99)
+    np.testing.assert_array_equal(got["experiments"], want["experiments"])
+    np.testing.assert_array_equal(got["responses"], want["responses"])
+    np.testing.assert_array_equal(got["pos"], want["pos"])
+    np.testing.assert_array_equal(got["neg"], want["neg"])
+    assert_posterior_close(lat.posterior(), want["posterior"], 6)
+
+
+def test_multinomial_update_masses(gpu, oracle):
+    rng = np.random.default_rng(77)
+    n, k = 7, 2
+    pi0 = rng.uniform(0.02, 0.3, n * k)
+    lat = bgt.Lattice(bgt.LatticeType.replicated_dilution, n, pi0, variants=k)
+    table = bgt.api.DilutionTable(n, 0.99, 0.005)
+    post = oracle.prior(pi0)
+    for step in range(3):
+        e = int(rng.integers(1, 1 << n))
+        r = int(rng.integers(0, 1 << k))
+        lat.update(e, r, table)
+        post = oracle.update(1, n, k, post, e, r)
+        assert_posterior_close(lat.posterior(), post, step + 1)
+        np.testing.assert_allclose(lat.atom_masses(), oracle.atom_masses(post, n * k), rtol=1e-12, atol=1e-18)
+        assert lat.select_experiment() == oracle.select(post, n, k, 0)

@@ -12,10 +12,10 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12
 
 
-def _run(dilution, n, pi0, depth, up=0.01, lo=0.01, branch=0.0, selector=0, alpha=0.99, h=0.005):
+def _run(dilution, n, pi0, depth, up=0.01, lo=0.01, branch=0.0, selector=0, alpha=0.99, h=0.005, k=1):
     cfg = bgt.SimulationConfig(
         lattice_type=bgt.LatticeType.replicated_dilution if dilution else bgt.LatticeType.replicated_non_dilution,
-        subjects=n, variants=1, prior=list(pi0),
+        subjects=n, variants=k, prior=list(pi0),
         options=bgt.SimulationOptions(search_depth=depth, threshold_up=up, threshold_lo=lo, branch_threshold=branch,
                                       selector=bgt.SelectorType(selector), provider=bgt.Provider.cuda),
         dilution=bgt.api.DilutionParameters(alpha, h))
@@ -56,4 +56,22 @@ def test_seeded_trees(gpu, oracle, n, depth, dil):
     pi0 = rng.uniform(0.01, 0.20, n)
     got = _run(dil, n, pi0, depth)
     want = oracle.run_simulation(1 if dil else 0, n, 1, pi0, depth)
+    _check(got, want)
+
+
+@pytest.mark.parametrize("case", [
+    # tests/cpp/integration/cuda_tree_parity_test.cpp:108-120 and :145-150
+    (False, 1, 2, [0.2, 0.4], 1, 0.01, 0.0, 0),
+    (False, 2, 2, [0.02, 0.04, 0.06, 0.08], 2, 0.01, 0.001, 2),
+    # tests/cpp/regression/no_shrink_tree_reference_test.cpp:356-377
+    (False, 2, 2, [0.2, 0.7, 0.4, 0.6], 2, 0.1, 0.0, 0),
+    (False, 6, 2, [0.02] * 12, 6, 0.01, 0.001, 0),
+    # seeded
+    (True, 4, 2, [0.03, 0.08, 0.05, 0.1, 0.02, 0.07, 0.04, 0.09], 4, 0.01, 0.0, 0),
+    (False, 4, 3, [0.02, 0.05, 0.08, 0.03, 0.06, 0.09, 0.04, 0.07, 0.1, 0.05, 0.02, 0.06], 3, 0.01, 0.0, 0),
+])
+def test_multinomial_trees(gpu, oracle, case):
+    dil, n, k, pi0, depth, thr, branch, sel = case
+    got = _run(dil, n, pi0, depth, thr, thr, branch, sel, k=k)
+    want = oracle.run_simulation(1 if dil else 0, n, k, pi0, depth, thr, thr, branch, sel)
     _check(got, want)
