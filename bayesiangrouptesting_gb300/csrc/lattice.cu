@@ -25,6 +25,7 @@ namespace bgt_gpu
 
 __global__ void k1_zeta_low(LatticeDev *states, int count, int per);
 __global__ void k2_zeta_high_select(LatticeDev *states, int count, int per);
+__global__ void kmid_zeta(LatticeDev *states, int count, int per);
 __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
 __global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, unsigned long long *out);
 
@@ -128,6 +129,8 @@ void configure_kernels()
 	cuda_check(cudaFuncSetAttribute(k2_zeta_high_select, cudaFuncAttributeMaxDynamicSharedMemorySize,
 									static_cast<int>(k2_smem_bytes(0))),
 			   "k2 smem attribute");
+	cuda_check(cudaFuncSetAttribute(kmid_zeta, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kPipeSmem)),
+			   "middle pass smem attribute");
 	done = true;
 }
 
@@ -142,10 +145,20 @@ void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 
 void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream)
 {
-	const long long items = static_cast<long long>(count) * g.nblk;
+	if (g.mbits > 0)
+	{
+		const int per_mid = g.nblk << g.mbits;
+		const long long mid_items = static_cast<long long>(count) * per_mid;
+		const int mgrid = static_cast<int>(std::min<long long>(mid_items, sm_count()));
+		timed_launch(1, stream, [&] { kmid_zeta<<<mgrid, kThreads, kPipeSmem, stream>>>(states, count, per_mid); });
+		cuda_check(cudaGetLastError(), "middle pass launch");
+		count_launches(1);
+	}
+	const int per = g.nblk << g.mbits;
+	const long long items = static_cast<long long>(count) * per;
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	timed_launch(1, stream,
-				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, count, g.nblk); });
+				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, count, per); });
 	cuda_check(cudaGetLastError(), "k2 launch");
 	count_launches(1);
 }
@@ -158,7 +171,8 @@ LatticeGeometry make_geometry(int n, int k)
 	g.atoms = n * k;
 	g.tbits = g.atoms < kTileBits ? g.atoms : kTileBits;
 	g.hbits = g.atoms - g.tbits;
-	int w = kTileElems >> g.hbits;
+	g.mbits = g.hbits > kMaxHighBits ? g.hbits - kMaxHighBits : 0;
+	int w = kTileElems >> (g.hbits - g.mbits);
 	w = std::max(w, kMinColW);
 	w = std::min(w, kMaxColW);
 	w = std::min(w, 1 << g.tbits);
@@ -183,11 +197,7 @@ int check_supported(int subjects, int variants, int dilution, std::string *why)
 		*why = "subjects * variants exceeds 30 atoms";
 		return BGT_GPU_UNSUPPORTED;
 	}
-	if (subjects * variants > kTileBits + kMaxHighBits)
-	{
-		*why = "lattices above 24 atoms (subjects * variants) are not supported by this build";
-		return BGT_GPU_UNSUPPORTED;
-	}
+
 	if (variants > 1)
 	{
 		long long entries = 1;
@@ -230,6 +240,7 @@ struct bgt_gpu_lattice
 	LatticeDev *dev = nullptr;  // device state
 	double *q = nullptr;
 	unsigned long long *m1 = nullptr;
+	unsigned long long *m2 = nullptr;
 	unsigned long long *tile_total = nullptr;
 	int *tile_scale = nullptr;
 	unsigned long long *blk_score = nullptr;
@@ -252,6 +263,7 @@ struct bgt_gpu_lattice
 		cudaFree(dev);
 		cudaFree(q);
 		cudaFree(m1);
+		cudaFree(m2);
 		cudaFree(tile_total);
 		cudaFree(tile_scale);
 		cudaFree(blk_score);
@@ -444,8 +456,12 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 					   "alloc zeta partials");
 			cuda_check(cudaMalloc(&lat->tile_total, rows * sizeof(unsigned long long)), "alloc tile totals");
 			cuda_check(cudaMalloc(&lat->tile_scale, rows * sizeof(int)), "alloc tile scales");
-			cuda_check(cudaMalloc(&lat->blk_score, g.nblk * sizeof(unsigned long long)), "alloc block scores");
-			cuda_check(cudaMalloc(&lat->blk_e, g.nblk * sizeof(unsigned int)), "alloc block winners");
+			cuda_check(cudaMalloc(&lat->blk_score, (static_cast<size_t>(g.nblk) << g.mbits) * sizeof(unsigned long long)),
+					   "alloc block scores");
+			cuda_check(cudaMalloc(&lat->blk_e, (static_cast<size_t>(g.nblk) << g.mbits) * sizeof(unsigned int)),
+					   "alloc block winners");
+			if (g.mbits > 0)
+				cuda_check(cudaMalloc(&lat->m2, states * sizeof(unsigned long long)), "alloc middle-pass partials");
 			cuda_check(cudaMalloc(&lat->dil, static_cast<size_t>(subjects) * (subjects + 1) * sizeof(double)),
 					   "alloc dilution");
 			cuda_check(cudaMalloc(&lat->prior_lo, (size_t{1} << g.tbits) * sizeof(double)), "alloc prior lo");
@@ -472,6 +488,8 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			h.nblk = g.nblk;
 			h.colw = g.colw;
 			h.logw = g.logw;
+			h.mbits = g.mbits;
+			h.m2 = lat->m2;
 			h.masses_in_k2 = 1;
 			h.dilution = lattice_type;
 			h.orig_n = subjects;

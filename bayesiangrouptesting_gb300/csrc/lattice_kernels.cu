@@ -146,15 +146,17 @@ __device__ __forceinline__ void argmin_block(u64 &s, unsigned int &e, u64 *ws, u
 struct LatCache
 {
 	int li;
-	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix;
+	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix, mbits;
 	unsigned int e, active;
 	const double *q_in;
 	double *q_out;
 	u64 *m1;
+	u64 *m2;
 	const double *prior_lo;
 	const double *prior_hi;
 	double c_in, c_out;
 	u64 zg;
+	int s_g;
 	int masses;
 	u64 *tile_total;
 	int *tile_scale;
@@ -547,6 +549,9 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.q_in = L.q_in;
 			c.q_out = L.q_out;
 			c.m1 = L.m1;
+			c.m2 = L.m2;
+			c.mbits = L.mbits;
+			c.s_g = L.s_g;
 			c.prior_lo = L.prior_lo;
 			c.prior_hi = L.prior_hi;
 			c.zg = L.z_g;
@@ -923,14 +928,15 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	auto issue = [&](long long item, int b) -> bool {
 		const int li = static_cast<int>(item / per);
 		const unsigned int blk = static_cast<unsigned int>(item % per);
-		int skip, hbits, colw;
-		u64 *m1;
+		int skip, hbits, colw, mbits;
+		u64 *src;
 		if (li == ps.lc.li)
 		{
 			skip = ps.lc.skip;
 			hbits = ps.lc.hbits;
 			colw = ps.lc.colw;
-			m1 = ps.lc.m1;
+			mbits = ps.lc.mbits;
+			src = mbits ? ps.lc.m2 : ps.lc.m1;
 		}
 		else
 		{
@@ -938,14 +944,15 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			skip = Ln.skip;
 			hbits = Ln.hbits;
 			colw = Ln.colw;
-			m1 = Ln.m1;
+			mbits = Ln.mbits;
+			src = mbits ? Ln.m2 : Ln.m1;
 		}
 		if (skip)
 			return false;
-		const uint32_t elems = (1u << hbits) * static_cast<uint32_t>(colw);
+		const uint32_t elems = (1u << (hbits - mbits)) * static_cast<uint32_t>(colw);
 		const uint32_t bytes = elems * 8u;
 		mbar_expect_tx(&ps.bars[b], bytes);
-		bulk_load(b ? inbuf1 : inbuf0, m1 + static_cast<size_t>(blk) * elems, bytes, &ps.bars[b]);
+		bulk_load(b ? inbuf1 : inbuf0, src + static_cast<size_t>(blk) * elems, bytes, &ps.bars[b]);
 		return true;
 	};
 	uint32_t parity0 = 0u, parity1 = 0u;
@@ -964,9 +971,11 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			const LatticeDev &Lc = states[li];
 			load_lattice_cache(Lc, li);
 			const int s_g = Lc.s_g;
-			const unsigned int rows_c = 1u << Lc.hbits;
+			// Rows of K1's partial sums carry tile scales; the middle pass's
+			// output is already at the global scale.
+			const unsigned int rows_c = 1u << (Lc.hbits - Lc.mbits);
 			for (unsigned int rr = tid; rr < rows_c; rr += kThreads)
-				shift[rr] = min(Lc.tile_scale[rr] - s_g, 63);
+				shift[rr] = Lc.mbits ? 0 : min(Lc.tile_scale[rr] - s_g, 63);
 			__syncthreads();
 		}
 		const long long wn = w + gridDim.x;
@@ -980,13 +989,17 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		}
 		if (ps.lc.skip)
 			continue;
-		const int tbits = ps.lc.tbits, logw = ps.lc.logw;
-		const unsigned int rows = 1u << ps.lc.hbits;
+		const int tbits = ps.lc.tbits, logw = ps.lc.logw, mbits = ps.lc.mbits;
+		const unsigned int rows = 1u << (ps.lc.hbits - mbits);
 		const unsigned int elems = rows << logw;
+		// Block index: column block and, above 24 atoms, the middle index.
+		const unsigned int r_lo = blk & ((1u << mbits) - 1u);
+		const unsigned int cblk = blk >> mbits;
+		const int row_shift = tbits + mbits;
 		const u64 zg = ps.lc.zg;
 		const unsigned int active = ps.lc.active;
 		const unsigned int all = ps.lc.n >= 32 ? 0xFFFFFFFFu : ((1u << ps.lc.n) - 1u);
-		const bool want_masses = ps.lc.masses != 0 && (blk & (blk - 1u)) == 0;
+		const bool want_masses = ps.lc.masses != 0 && ((blk >> ps.lc.mbits) & ((blk >> ps.lc.mbits) - 1u)) == 0;
 		const bool timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);
 		if (b)
 			parity1 ^= 1u;
@@ -1047,7 +1060,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		// All row bits are done (W >= 4, so y bits 0..1 are column bits).
 		// Score |2 M(E) - Z_g|; within a thread E grows with j, so a strict
 		// comparison keeps the lowest index on ties.
-		const unsigned int col_base = blk << logw;
+		const unsigned int col_base = (r_lo << tbits) | (cblk << logw);
 		const unsigned int wmask = (1u << logw) - 1u;
 		const unsigned int y0 = map_c(tid, 0);
 		u64 best = ~0ull;
@@ -1066,7 +1079,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 				const unsigned int y = y0 + (j << 2);
 				if (y >= elems)
 					continue;
-				const unsigned int Eall = ((y >> logw) << tbits) | col_base | (y & wmask);
+				const unsigned int Eall = ((y >> logw) << row_shift) | col_base | (y & wmask);
 				unsigned int ev = 0, bset = 0;
 				bool diag = true;
 				for (int v = 0; v < kk; v++)
@@ -1101,7 +1114,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			for (int j = 0; j < kPerThread; j++)
 			{
 				const unsigned int y = y0 + (j << 2);
-				const unsigned int E = ((y >> logw) << tbits) | col_base | (y & wmask);
+				const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
 				const u64 m2 = a[j] << 1;
 				const u64 score = m2 > zg ? m2 - zg : zg - m2;
 				const bool take = y < elems && (E & ~active) == 0 && score < best;
@@ -1113,7 +1126,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		if (best_j >= 0)
 		{
 			const unsigned int y = y0 + (best_j << 2);
-			best_e = ((y >> logw) << tbits) | col_base | (y & wmask);
+			best_e = ((y >> logw) << row_shift) | col_base | (y & wmask);
 		}
 		LatticeDev &L = states[li];
 		// Singleton (atom) masses live in block 0 and in the blocks whose
@@ -1124,7 +1137,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			for (int j = 0; j < kPerThread; j++)
 			{
 				const unsigned int y = y0 + (j << 2);
-				const unsigned int E = ((y >> logw) << tbits) | col_base | (y & wmask);
+				const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
 				if (y < elems && __popc(E) == 1)
 					L.atom_fixed[__ffs(E) - 1] = a[j];
 			}
@@ -1153,6 +1166,142 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 				k2_epilogue(L, per);
 			}
 		}
+	}
+}
+
+// Middle pass, for lattices above 24 atoms.  Work item i of a lattice is
+// column block i >> mbits and part i & (2^mbits - 1): 2048 consecutive tile
+// rows x 4 columns of K1's partial sums (one contiguous 64 KB chunk, bulk
+// copied and double-buffered like K2).  Each row is rescaled to the global
+// scale, the zeta runs over the low mbits bits of the tile index (block
+// index bits 2 .. 2 + mbits), and the values are written transposed,
+// [column block][r_lo][r_hi][4], so that K2's blocks stay contiguous.
+__global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, int count, int per)
+{
+	u64 *const inbuf0 = tile_u64(0);
+	u64 *const inbuf1 = tile_u64(1);
+	u64 *const work = work_tile();
+	const unsigned int tid = threadIdx.x;
+	const long long total = static_cast<long long>(count) * per;
+	long long w = blockIdx.x;
+	if (w >= total)
+		return;
+	if (tid == 0)
+	{
+		mbar_init(&ps.bars[0], 1);
+		mbar_init(&ps.bars[1], 1);
+		mbar_init_fence();
+		ps.lc.li = -1;
+	}
+	__syncthreads();
+	auto issue = [&](long long item, int b) -> bool {
+		const LatticeDev &Ln = states[item / per];
+		const unsigned int i = static_cast<unsigned int>(item % per);
+		mbar_expect_tx(&ps.bars[b], kTileElems * 8u);
+		bulk_load(b ? inbuf1 : inbuf0, Ln.m1 + static_cast<size_t>(i) * kTileElems, kTileElems * 8u, &ps.bars[b]);
+		return true;
+	};
+	uint32_t parity0 = 0u, parity1 = 0u;
+	bool inflight0 = false, inflight1 = false;
+	if (tid == 0)
+		inflight0 = issue(w, 0);
+	for (int it = 0; w < total; w += gridDim.x, it++)
+	{
+		const int b = it & 1;
+		const int li = static_cast<int>(w / per);
+		const unsigned int item = static_cast<unsigned int>(w % per);
+		if (li != ps.lc.li)
+		{
+			__syncthreads();
+			load_lattice_cache(states[li], li);
+			__syncthreads();
+		}
+		const long long wn = w + gridDim.x;
+		if (tid == 0 && wn < total)
+		{
+			proxy_fence();
+			if (b)
+				inflight0 = issue(wn, 0);
+			else
+				inflight1 = issue(wn, 1);
+		}
+		const int mbits = ps.lc.mbits;
+		const int h2 = ps.lc.hbits - mbits;
+		const int s_g = ps.lc.s_g;
+		const int *tile_scale = ps.lc.tile_scale;
+		u64 *const m2 = ps.lc.m2;
+		const unsigned int cblk = item >> mbits;
+		const unsigned int part = item & ((1u << mbits) - 1u);
+		const unsigned int row0 = part << 11; // first tile row of this chunk
+		const bool timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);
+		if (b)
+			parity1 ^= 1u;
+		else
+			parity0 ^= 1u;
+		if (tid == 0)
+		{
+			if (b)
+				inflight1 = false;
+			else
+				inflight0 = false;
+		}
+		const u64 *in = b ? inbuf1 : inbuf0;
+		const unsigned int mask = ((1u << mbits) - 1u) << 2;
+		u64 a[kPerThread];
+#pragma unroll
+		for (int i = 0; i < kPerThread / 2; i++)
+		{
+			const unsigned int y = map_a(tid, 2 * i);
+			ulonglong2 p = *reinterpret_cast<const ulonglong2 *>(in + y);
+			const int rs = min(__ldg(tile_scale + row0 + (y >> 2)) - s_g, 63);
+			a[2 * i] = shr_round(p.x, rs);
+			a[2 * i + 1] = shr_round(p.y, rs);
+		}
+		levels_a(a, mask);
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			work[tile_swz(map_a(tid, j))] = a[j];
+		if (__syncthreads_or(timed_out))
+		{
+			if (tid == 0)
+			{
+				atomicExch(&states[li].error, kErrTimeout);
+				if (b ? inflight0 : inflight1)
+					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
+			}
+			return;
+		}
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			a[j] = work[tile_swz(map_b(tid, j))];
+		levels_b(a, mask);
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			work[tile_swz(map_b(tid, j))] = a[j];
+		__syncthreads();
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			a[j] = work[tile_swz(map_c(tid, j))];
+		levels_c(a, mask);
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			work[tile_swz(map_c(tid, j))] = a[j];
+		__syncthreads();
+		// Thread t now takes block indices 16 t .. 16 t + 15: four rows of
+		// four columns, each row one 32-byte sector of the transposed output.
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			a[j] = work[tile_swz(map_d(tid, j))];
+#pragma unroll
+		for (int q = 0; q < 4; q++)
+		{
+			const unsigned int r = row0 + 4u * tid + q;
+			const unsigned int r_lo = r & ((1u << mbits) - 1u);
+			const unsigned int r_hi = r >> mbits;
+			u64 *dst = m2 + ((((static_cast<size_t>(cblk) << mbits) | r_lo) << h2) | r_hi) * 4u;
+			st_global_v4_u64(dst, a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+		}
+		__syncthreads();
 	}
 }
 

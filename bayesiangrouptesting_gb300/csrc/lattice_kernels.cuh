@@ -54,6 +54,7 @@ constexpr int kPerThread = kTileElems / kThreads;
 constexpr int kMaxColW = 16;                  // K2 block columns (u64 values per M1 row chunk)
 constexpr int kMinColW = 4;                   // 32-byte row chunks at the least
 constexpr int kMaxHighBits = 11;              // K2 block = 2^h rows x W columns <= 2^13 values
+constexpr int kMaxMidBits = 6;                // middle pass: 13 + 6 + 11 = 30 atoms
 constexpr int kMaxAtoms = 30;
 constexpr int kMaxClasses = 32;               // likelihood classes for k = 1 (popcount 0..n)
 constexpr int kMaxClassTable = 4096;          // mixed-radix likelihood classes for k >= 2
@@ -79,12 +80,14 @@ struct LatticeDev
 	int nblk;     // K2 column blocks (2^tbits / colw)
 	int colw;     // K2 block columns W
 	int logw;     // log2(W)
+	int mbits;    // lattices above 24 atoms: tile-index bits transformed by the middle pass
 	int dilution; // 0 / 1
 	int orig_n;   // subjects of the dilution table
 	// ---- buffers (host-set) ----
 	const double *q_in;
 	double *q_out;
-	unsigned long long *m1;        // [nblk][2^hbits][16]
+	unsigned long long *m1;        // [nblk][2^hbits][W]
+	unsigned long long *m2;        // mbits > 0: [nblk][2^mbits][2^(hbits - mbits)][W], global scale
 	unsigned long long *tile_total; // [2^hbits]
 	int *tile_scale;               // [2^hbits]
 	unsigned long long *blk_score; // [nblk]

@@ -86,11 +86,13 @@ __global__ void noalloc_setup(const double *posterior, LatticeGeometry g)
 	L.nblk = g.nblk;
 	L.colw = g.colw;
 	L.logw = g.logw;
+	L.mbits = 0;
 	L.dilution = 0;
 	L.orig_n = g.n;
 	L.q_in = posterior;
 	L.q_out = nullptr;
 	L.m1 = s.m1;
+	L.m2 = nullptr;
 	L.tile_total = s.tile_total;
 	L.tile_scale = s.tile_scale;
 	L.blk_score = s.blk_score;

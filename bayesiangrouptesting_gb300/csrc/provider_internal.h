@@ -21,7 +21,7 @@ struct CudaFailure : std::runtime_error
 
 struct LatticeGeometry
 {
-	int n = 0, k = 1, atoms = 0, tbits = 0, hbits = 0, nblk = 1, colw = 1, logw = 0;
+	int n = 0, k = 1, atoms = 0, tbits = 0, hbits = 0, nblk = 1, colw = 1, logw = 0, mbits = 0;
 };
 
 void set_error(const std::string &message);

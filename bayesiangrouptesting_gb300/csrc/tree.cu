@@ -195,6 +195,7 @@ struct Level
 	LatticeDev *states = nullptr; // device array, one per node
 	double *q = nullptr;          // posteriors, one 2^A slice per node
 	unsigned long long *m1 = nullptr;
+	unsigned long long *m2 = nullptr;
 	unsigned long long *tile_total = nullptr;
 	int *tile_scale = nullptr;
 	unsigned long long *blk_score = nullptr;
@@ -207,6 +208,8 @@ struct Level
 		cudaFree(states);
 		cudaFree(q);
 		cudaFree(m1);
+		cudaFree(m2);
+		m2 = nullptr;
 		cudaFree(tile_total);
 		cudaFree(tile_scale);
 		cudaFree(blk_score);
@@ -240,8 +243,11 @@ void allocate_level(Level &lv, const LatticeGeometry &g)
 			   "alloc tree zeta partials");
 	cuda_check(cudaMalloc(&lv.tile_total, count * rows * sizeof(unsigned long long)), "alloc tile totals");
 	cuda_check(cudaMalloc(&lv.tile_scale, count * rows * sizeof(int)), "alloc tile scales");
-	cuda_check(cudaMalloc(&lv.blk_score, count * g.nblk * sizeof(unsigned long long)), "alloc block scores");
-	cuda_check(cudaMalloc(&lv.blk_e, count * g.nblk * sizeof(unsigned int)), "alloc block winners");
+	cuda_check(cudaMalloc(&lv.blk_score, (count * g.nblk << g.mbits) * sizeof(unsigned long long)),
+			   "alloc block scores");
+	cuda_check(cudaMalloc(&lv.blk_e, (count * g.nblk << g.mbits) * sizeof(unsigned int)), "alloc block winners");
+	if (g.mbits > 0)
+		cuda_check(cudaMalloc(&lv.m2, count * states * sizeof(unsigned long long)), "alloc middle-pass partials");
 	if (g.k > 1)
 		cuda_check(cudaMalloc(&lv.ftab, count * (size_t{1} << (g.n + g.k)) * sizeof(unsigned long long)),
 				   "alloc feature masses");
@@ -256,8 +262,9 @@ void bind_level_buffers(Level &lv, const LatticeGeometry &g, size_t i, LatticeDe
 	d.m1 = lv.m1 + i * static_cast<size_t>(g.nblk) * rows * g.colw;
 	d.tile_total = lv.tile_total + i * rows;
 	d.tile_scale = lv.tile_scale + i * rows;
-	d.blk_score = lv.blk_score + i * g.nblk;
-	d.blk_e = lv.blk_e + i * g.nblk;
+	d.blk_score = lv.blk_score + (i * g.nblk << g.mbits);
+	d.blk_e = lv.blk_e + (i * g.nblk << g.mbits);
+	d.m2 = lv.m2 ? lv.m2 + i * states : nullptr;
 	d.ftab = lv.ftab ? lv.ftab + i * (size_t{1} << (g.n + g.k)) : nullptr;
 }
 
@@ -333,6 +340,7 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 		d.nblk = g.nblk;
 		d.colw = g.colw;
 		d.logw = g.logw;
+		d.mbits = g.mbits;
 		d.masses_in_k2 = 0;
 		d.dilution = use_dilution;
 		d.orig_n = subjects;
@@ -450,6 +458,7 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 		next.blk_score = nullptr;
 		next.blk_e = nullptr;
 		next.ftab = nullptr;
+		next.m2 = nullptr;
 	}
 	prev.release();
 	cur.release();

@@ -1,0 +1,103 @@
+"""Lattices above 24 atoms, where the zeta runs in three passes (13 tile bits,
+then up to 6 middle bits, then the top 11 bits).
+
+At 25 and 26 atoms the device is compared with the oracle directly (an
+adaptive dilution session; a two-variant multinomial session).  From 27 to 30
+atoms the oracle takes minutes, so the checks use a property that holds at
+any size: after one non-dilution update of a product prior, the upset mass of
+every experiment has a closed form (a mixture of two products), so the
+optimal Op-BHA score can be found by brute force on the host and the device's
+selection and atom masses checked against it."""
+import numpy as np
+import pytest
+
+import bayesiangrouptesting_gb300 as bgt
+from conftest import assert_posterior_close
+
+pytestmark = pytest.mark.gpu
+
+
+def test_dilution_session_25_atoms_matches_oracle(gpu, oracle):
+    rng = np.random.default_rng(2525)
+    n = 25
+    pi0 = rng.uniform(0.005, 0.1, n)
+    truth = int(rng.integers(0, 1 << n))
+    lat = bgt.Lattice(bgt.LatticeType.replicated_dilution, n, pi0)
+    got = lat.run_session(2, truth, seed=11, session=3, selector=bgt.SelectorType.op_bbpa, alpha=0.01, h=0.005)
+    want = oracle.session(1, n, 1, pi0, 2, 11, 3, truth, selector=2, alpha=0.01, h=0.005)
+    for key in ("experiments", "responses", "pos", "neg"):
+        np.testing.assert_array_equal(got[key], want[key])
+    assert_posterior_close(lat.posterior(), want["posterior"], 2)
+
+
+def test_multinomial_session_26_atoms_matches_oracle(gpu, oracle):
+    rng = np.random.default_rng(2626)
+    n, k = 13, 2
+    pi0 = rng.uniform(0.01, 0.2, n * k)
+    truth = int(rng.integers(0, 1 << (n * k)))
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0, variants=k)
+    got = lat.run_session(1, truth, seed=5, session=1, selector=bgt.SelectorType.op_bbpa, alpha=0.99)
+    want = oracle.session(0, n, k, pi0, 1, 5, 1, truth, selector=2, alpha=0.99)
+    for key in ("experiments", "responses", "pos", "neg"):
+        np.testing.assert_array_equal(got[key], want[key])
+    assert_posterior_close(lat.posterior(), want["posterior"], 1)
+
+
+def _closed_form_scores(n, pi0, e0, l_in, l_out, chunk_rows=256):
+    """Upset mass M(E) = P(every subject of E negative) after one update of the
+    product prior: q(s) ~ prior(s) * (l_in if s contains e0 else l_out), with
+    internal bit 1 = negative.  Returns (best score |2 M - 1|, M function)."""
+    neg = 1.0 - np.asarray(pi0)
+    lo_bits = min(n, 15)
+    hi_bits = n - lo_bits
+
+    def table(bits, offset):
+        t = np.ones(1 << bits)
+        for j in range(bits):
+            t[1 << j:2 << j] = t[:1 << j] * neg[offset + j]
+        return t
+
+    a_lo, a_hi = table(lo_bits, 0), table(hi_bits, lo_bits)
+    idx_lo = np.arange(1 << lo_bits)
+    e_lo, e_hi = e0 & ((1 << lo_bits) - 1), e0 >> lo_bits
+
+    def prod(x):
+        return a_hi[x >> lo_bits] * a_lo[x & ((1 << lo_bits) - 1)]
+
+    z = l_in * prod(e0) + l_out * (1.0 - prod(e0))
+
+    def mass(e):
+        both = prod(e | e0)
+        return (l_in * both + l_out * (prod(e) - both)) / z
+
+    best = np.inf
+    b_lo = a_lo[idx_lo | e_lo]
+    for h0 in range(0, 1 << hi_bits, chunk_rows):
+        h = np.arange(h0, min(h0 + chunk_rows, 1 << hi_bits))
+        plain = np.outer(a_hi[h], a_lo)
+        both = np.outer(a_hi[h | e_hi], b_lo)
+        m = (l_in * both + l_out * (plain - both)) / z
+        best = min(best, float(np.min(np.abs(2.0 * m - 1.0))))
+    return best, mass
+
+
+@pytest.mark.parametrize("n", [27, 29, 30])
+def test_selection_above_24_atoms_closed_form(gpu, oracle, n):
+    rng = np.random.default_rng(3000 + n)
+    pi0 = rng.uniform(0.01, 0.15, n)
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0)
+    # The prior itself: atom masses are 1 - pi0 (internal order).
+    np.testing.assert_allclose(lat.atom_masses(), 1.0 - pi0, rtol=0, atol=1e-12)
+    e0 = int(rng.integers(1, 1 << n))
+    r = 1
+    lat.update(bgt.reverse_bits(e0, n), r)
+    l_in = oracle.response_prob(0, n, 1, e0, r, (1 << n) - 1)
+    l_out = oracle.response_prob(0, n, 1, e0, r, 0)
+    best, mass = _closed_form_scores(n, pi0, e0, l_in, l_out)
+    for sel in (bgt.SelectorType.op_bha, bgt.SelectorType.op_bbpa):
+        e = bgt.reverse_bits(lat.select_experiment(sel), n)
+        score = abs(2.0 * mass(e) - 1.0)
+        assert score <= best + 1e-12, (sel, e, score, best)
+        assert abs(lat.upset_probability_mass(bgt.reverse_bits(e, n)) - mass(e)) <= 1e-12
+    want = np.array([mass(1 << j) for j in range(n)])
+    np.testing.assert_allclose(lat.atom_masses(), want, rtol=0, atol=1e-12)

@@ -119,3 +119,21 @@ def test_randomized_bit_exact_against_reference(oracle):
         pi0 = rng.uniform(0.01, 0.2, n)
         np.testing.assert_array_equal(oracle.run_simulation(dil, n, 1, pi0, depth),
                                       ref.run_simulation(dil, n, 1, pi0, depth))
+
+
+def test_closed_form_upset_masses_match_oracle(oracle):
+    # The closed form used for the 27-30 atom device checks, pinned against
+    # the oracle's own zeta on small lattices.
+    from test_gpu_large import _closed_form_scores
+
+    rng = np.random.default_rng(5)
+    for n in (9, 12):
+        pi0 = rng.uniform(0.01, 0.15, n)
+        e0 = int(rng.integers(1, 1 << n))
+        post = oracle.update(0, n, 1, oracle.prior(pi0), e0, 1)
+        e, upset = oracle.op_bha(post, n)
+        l_in = oracle.response_prob(0, n, 1, e0, 1, (1 << n) - 1)
+        l_out = oracle.response_prob(0, n, 1, e0, 1, 0)
+        best, mass = _closed_form_scores(n, pi0, e0, l_in, l_out)
+        np.testing.assert_allclose([mass(x) for x in range(1 << n)], upset, rtol=0, atol=1e-14)
+        assert abs(best - abs(2.0 * upset[e] - 1.0)) <= 1e-14
