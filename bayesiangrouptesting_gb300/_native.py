@@ -32,7 +32,54 @@ class TreeStatsC(ctypes.Structure):
     ]
 
 
-# Every symbol the header declares, with its ctypes signature.
+class ServeConfigC(ctypes.Structure):
+    """Layout of bgt_serve_config (include/bgt_serve.h)."""
+
+    _fields_ = [
+        ("memory_budget", c_uint64),
+        ("max_sessions", c_int),
+        ("max_stages", c_int),
+        ("threshold_up", c_double),
+        ("threshold_lo", c_double),
+    ]
+
+
+class ServeRequestC(ctypes.Structure):
+    """Layout of bgt_serve_request (include/bgt_serve.h)."""
+
+    _fields_ = [
+        ("dilution", c_int),
+        ("subjects", c_int),
+        ("prior", POINTER(c_double)),
+        ("alpha", c_double),
+        ("h", c_double),
+        ("selector", c_int),
+        ("seed", c_uint64),
+        ("session", c_uint64),
+        ("true_state", c_uint32),
+    ]
+
+
+class ServeResultC(ctypes.Structure):
+    """Layout of bgt_serve_result (include/bgt_serve.h)."""
+
+    _fields_ = [
+        ("ticket", c_uint64),
+        ("subjects", c_int),
+        ("stages", c_int),
+        ("error", c_int),
+        ("positive_mask", c_uint32),
+        ("negative_mask", c_uint32),
+        ("submit_s", c_double),
+        ("admit_s", c_double),
+        ("finish_s", c_double),
+        ("rounds", c_int),
+    ]
+
+
+_ip = POINTER(c_int)
+
+# Every symbol the headers declare, with its ctypes signature.
 SIGNATURES = {
     "bgt_cuda_provider_available": ([], c_int),
     "bgt_cuda_provider_run": ([c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_int,
@@ -52,6 +99,14 @@ SIGNATURES = {
     "bgt_gpu_lattice_atom_masses": ([c_void_p, _dp], c_int),
     "bgt_gpu_session_run": ([c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_uint64, c_uint64,
                              c_uint32, _up, _up, _up, _up], c_int),
+    "bgt_gpu_session_run_until_classified": ([c_void_p, c_int, c_int, c_double, c_double, c_double, c_double,
+                                              c_uint64, c_uint64, c_uint32, _up, _up, _up, _up, _ip], c_int),
+    "bgt_gpu_server_create": ([POINTER(ServeConfigC), POINTER(c_void_p)], c_int),
+    "bgt_gpu_server_destroy": ([c_void_p], c_int),
+    "bgt_gpu_server_submit": ([c_void_p, POINTER(ServeRequestC), POINTER(c_uint64)], c_int),
+    "bgt_gpu_server_step": ([c_void_p, _ip, _ip, _ip], c_int),
+    "bgt_gpu_server_result": ([c_void_p, c_uint64, POINTER(ServeResultC), _up, _up, _up, _up, c_int], c_int),
+    "bgt_gpu_server_rounds": ([c_void_p, c_int, c_int, _dp, _dp, _ip, _ip], c_int),
     "bgt_gpu_lattice_reset": ([c_void_p, _dp], c_int),
     "bgt_gpu_profile_enable": ([c_int], c_int),
     "bgt_gpu_profile_read": ([POINTER(c_uint64), _dp], c_int),

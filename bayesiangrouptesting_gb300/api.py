@@ -386,6 +386,27 @@ class Lattice:
         return dict(experiments=ex, responses=rs, pos=pm, neg=nm)
 
 
+    def run_session_until_classified(self, max_stages: int, true_state: int, seed: int, session: int = 0,
+                                     selector: SelectorType = SelectorType.auto_select, alpha: float = 0.99,
+                                     h: float = 0.005, threshold_up: float = 0.01, threshold_lo: float = 0.01):
+        """Device-driven session that ends once every atom is classified
+        (bgt_gpu_session_run_until_classified); internal bit order.  The
+        arrays hold the stages run."""
+        ex = np.zeros(max_stages, np.uint32)
+        rs = np.zeros(max_stages, np.uint32)
+        pm = np.zeros(max_stages, np.uint32)
+        nm = np.zeros(max_stages, np.uint32)
+        ran = ctypes.c_int()
+        _call(self._lib.bgt_gpu_session_run_until_classified(
+            self._handle, int(selector), max_stages, alpha, h, threshold_up, threshold_lo, seed, session, true_state,
+            ex.ctypes.data_as(_up), rs.ctypes.data_as(_up), pm.ctypes.data_as(_up), nm.ctypes.data_as(_up),
+            ctypes.byref(ran)))
+        n = ran.value
+        if n:
+            self._pos, self._neg = int(pm[n - 1]), int(nm[n - 1])
+        return dict(experiments=ex[:n], responses=rs[:n], pos=pm[:n], neg=nm[:n], stages=n)
+
+
 def select_experiment(lattice: Lattice, selector: SelectorType = SelectorType.auto_select) -> int:
     return lattice.select_experiment(selector)
 

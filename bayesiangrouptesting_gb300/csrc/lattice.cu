@@ -23,9 +23,9 @@
 namespace bgt_gpu
 {
 
-__global__ void k1_zeta_low(LatticeDev *states, int count, int per);
-__global__ void k2_zeta_high_select(LatticeDev *states, int count, int per);
-__global__ void kmid_zeta(LatticeDev *states, int count, int per);
+__global__ void k1_zeta_low(LatticeDev *states, WorkMap wm);
+__global__ void k2_zeta_high_select(LatticeDev *states, WorkMap wm);
+__global__ void kmid_zeta(LatticeDev *states, WorkMap wm);
 __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
 __global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, unsigned long long *out);
 
@@ -138,7 +138,8 @@ void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 {
 	const long long items = static_cast<long long>(count) << g.hbits;
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
-	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, count, 1 << g.hbits); });
+	const WorkMap wm{count, 1 << g.hbits, nullptr, nullptr};
+	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, wm); });
 	cuda_check(cudaGetLastError(), "k1 launch");
 	count_launches(1);
 }
@@ -150,20 +151,51 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 		const int per_mid = g.nblk << g.mbits;
 		const long long mid_items = static_cast<long long>(count) * per_mid;
 		const int mgrid = static_cast<int>(std::min<long long>(mid_items, sm_count()));
-		timed_launch(1, stream, [&] { kmid_zeta<<<mgrid, kThreads, kPipeSmem, stream>>>(states, count, per_mid); });
+		const WorkMap wm_mid{count, per_mid, nullptr, nullptr};
+		timed_launch(1, stream, [&] { kmid_zeta<<<mgrid, kThreads, kPipeSmem, stream>>>(states, wm_mid); });
 		cuda_check(cudaGetLastError(), "middle pass launch");
 		count_launches(1);
 	}
 	const int per = g.nblk << g.mbits;
 	const long long items = static_cast<long long>(count) * per;
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	const WorkMap wm{count, per, nullptr, nullptr};
 	timed_launch(1, stream,
-				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, count, per); });
+				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, wm); });
 	cuda_check(cudaGetLastError(), "k2 launch");
 	count_launches(1);
 }
 
-LatticeGeometry make_geometry(int n, int k)
+void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream)
+{
+	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, wm); });
+	cuda_check(cudaGetLastError(), "k1 launch");
+	count_launches(1);
+}
+
+void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream)
+{
+	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	timed_launch(1, stream, [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(0), stream>>>(states, wm); });
+	cuda_check(cudaGetLastError(), "k2 launch");
+	count_launches(1);
+}
+
+void dilution_rows(int n, double alpha, double h, double *flat)
+{
+	for (int L = 1; L <= n; L++)
+	{
+		flat[static_cast<size_t>(L - 1) * (n + 1)] = alpha;
+		for (int r = 1; r <= L; r++)
+		{
+			const int kk = L - r;
+			flat[static_cast<size_t>(L - 1) * (n + 1) + r] = 1 - alpha * r / (kk * h + r);
+		}
+	}
+}
+
+LatticeGeometry make_geometry(int n, int k, bool wide)
 {
 	LatticeGeometry g;
 	g.n = n;
@@ -174,7 +206,8 @@ LatticeGeometry make_geometry(int n, int k)
 	g.mbits = g.hbits > kMaxHighBits ? g.hbits - kMaxHighBits : 0;
 	int w = kTileElems >> (g.hbits - g.mbits);
 	w = std::max(w, kMinColW);
-	w = std::min(w, kMaxColW);
+	if (!wide)
+		w = std::min(w, kMaxColW);
 	w = std::min(w, 1 << g.tbits);
 	g.colw = w;
 	g.logw = 0;
@@ -775,11 +808,21 @@ int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, do
 	});
 }
 
-int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, double alpha, double h,
-						double threshold_up, double threshold_lo, uint64_t seed, uint64_t session,
-						uint32_t true_state, uint32_t *experiments, uint32_t *responses, uint32_t *positive_masks,
-						uint32_t *negative_masks)
+} // extern "C"
+
+namespace
 {
+
+// The device-driven session loop shared by both session entry points.  With
+// `stop`, the session ends after the stage whose classification covers every
+// atom; the passes still launched after that return at once.
+int session_run_impl(bgt_gpu_lattice *lattice, int selector, int stages, double alpha, double h, double threshold_up,
+					 double threshold_lo, uint64_t seed, uint64_t session, uint32_t true_state, uint32_t *experiments,
+					 uint32_t *responses, uint32_t *positive_masks, uint32_t *negative_masks, bool stop,
+					 int *stages_run)
+{
+	if (stages_run)
+		*stages_run = 0;
 	if (!lattice)
 	{
 		set_error("null lattice");
@@ -810,15 +853,7 @@ int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, doub
 		if (lattice->dilution)
 		{
 			std::vector<double> flat(static_cast<size_t>(lattice->g.n) * (lattice->g.n + 1), 0.0);
-			for (int L = 1; L <= lattice->g.n; L++)
-			{
-				flat[static_cast<size_t>(L - 1) * (lattice->g.n + 1)] = alpha;
-				for (int r = 1; r <= L; r++)
-				{
-					const int kk = L - r;
-					flat[static_cast<size_t>(L - 1) * (lattice->g.n + 1) + r] = 1 - alpha * r / (kk * h + r);
-				}
-			}
+			dilution_rows(lattice->g.n, alpha, h, flat.data());
 			cuda_check(cudaMemcpyAsync(lattice->dil, flat.data(), flat.size() * sizeof(double), cudaMemcpyHostToDevice,
 									   lattice->stream),
 					   "dilution upload");
@@ -844,8 +879,10 @@ int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, doub
 		hst.out_r = o + S;
 		hst.out_pos = o + 2 * S;
 		hst.out_neg = o + 3 * S;
+		hst.sess_stop = stop ? 1 : 0;
+		hst.status = nullptr;
 		const size_t first = offsetof(LatticeDev, sess_active);
-		const size_t last = offsetof(LatticeDev, out_neg) + sizeof(unsigned int *);
+		const size_t last = offsetof(LatticeDev, status) + sizeof(SessionStatus *);
 		cuda_check(cudaMemcpyAsync(reinterpret_cast<char *>(lattice->dev) + first,
 								   reinterpret_cast<const char *>(&hst) + first, last - first, cudaMemcpyHostToDevice,
 								   lattice->stream),
@@ -867,10 +904,20 @@ int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, doub
 		cuda_check(cudaMemcpyAsync(host.data(), o, host.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost,
 								   lattice->stream),
 				   "session read");
-		cuda_check(cudaStreamSynchronize(lattice->stream), "session sync");
+		const int ran = lattice->get_field<int>(offsetof(LatticeDev, stage)); // synchronises
 		lattice->check_device_error();
-		lattice->pos = host[2 * S + S - 1];
-		lattice->neg = host[3 * S + S - 1];
+		if (stop)
+		{
+			// The lattice stays usable for single calls after the session.
+			lattice->set_field(offsetof(LatticeDev, skip), 0);
+			lattice->set_field(offsetof(LatticeDev, sess_stop), 0);
+			hst.sess_stop = 0;
+		}
+		if (stages_run)
+			*stages_run = ran;
+		const size_t lastst = static_cast<size_t>(ran > 0 ? ran - 1 : 0);
+		lattice->pos = ran > 0 ? host[2 * S + lastst] : lattice->pos;
+		lattice->neg = ran > 0 ? host[3 * S + lastst] : lattice->neg;
 		if (experiments)
 			std::memcpy(experiments, host.data(), S * sizeof(uint32_t));
 		if (responses)
@@ -881,6 +928,29 @@ int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, doub
 			std::memcpy(negative_masks, host.data() + 3 * S, S * sizeof(uint32_t));
 		return BGT_GPU_OK;
 	});
+}
+
+} // namespace
+
+extern "C" {
+
+int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int stages, double alpha, double h,
+						double threshold_up, double threshold_lo, uint64_t seed, uint64_t session,
+						uint32_t true_state, uint32_t *experiments, uint32_t *responses, uint32_t *positive_masks,
+						uint32_t *negative_masks)
+{
+	return session_run_impl(lattice, selector, stages, alpha, h, threshold_up, threshold_lo, seed, session, true_state,
+							experiments, responses, positive_masks, negative_masks, false, nullptr);
+}
+
+int bgt_gpu_session_run_until_classified(bgt_gpu_lattice *lattice, int selector, int max_stages, double alpha,
+										 double h, double threshold_up, double threshold_lo, uint64_t seed,
+										 uint64_t session, uint32_t true_state, uint32_t *experiments,
+										 uint32_t *responses, uint32_t *positive_masks, uint32_t *negative_masks,
+										 int *stages_run)
+{
+	return session_run_impl(lattice, selector, max_stages, alpha, h, threshold_up, threshold_lo, seed, session,
+							true_state, experiments, responses, positive_masks, negative_masks, true, stages_run);
 }
 
 } // extern "C"

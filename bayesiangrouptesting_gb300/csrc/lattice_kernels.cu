@@ -566,13 +566,13 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 }
 
 // K1: [update] -> per-tile fixed point -> zeta over the low t bits -> M1.
-// Grid: persistent, at most one CTA per work item; `per` = tiles per lattice.
-__global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, int count, int per)
+// Grid: persistent, at most one CTA per work item; an item is one tile.
+__global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, WorkMap wm)
 {
 	double *const inbuf0 = tile_f64(0);
 	double *const inbuf1 = tile_f64(1);
 	const unsigned int tid = threadIdx.x;
-	const long long total = static_cast<long long>(count) * per;
+	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
 		return;
@@ -583,30 +583,37 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 		mbar_init_fence();
 		ps.flag = 0;
 	}
-	load_lattice_cache(states[w / per], static_cast<int>(w / per));
-	load_class_table(states[w / per]);
+	{
+		unsigned int i0, n0;
+		const int l0 = wm_find(wm, w, i0, n0);
+		load_lattice_cache(wm_state(states, wm, l0), l0);
+		load_class_table(wm_state(states, wm, l0));
+	}
 	__syncthreads();
 	// Thread 0 issues the bulk copy of item `item` into buffer b (no copy
-	// for generated priors); same-lattice items use the cached constants.
+	// for generated priors or skipped lattices); same-lattice items use the
+	// cached constants.
 	auto issue = [&](long long item, int b) -> bool {
-		const int li = static_cast<int>(item / per);
-		const unsigned int rn = static_cast<unsigned int>(item % per);
-		int mode, tbits;
+		unsigned int rn, rcount;
+		const int li = wm_find(wm, item, rn, rcount);
+		int mode, tbits, skip;
 		const double *q_in;
 		if (li == ps.lc.li)
 		{
 			mode = ps.lc.mode;
 			tbits = ps.lc.tbits;
 			q_in = ps.lc.q_in;
+			skip = ps.lc.skip;
 		}
 		else
 		{
-			const LatticeDev &Ln = states[li];
+			const LatticeDev &Ln = wm_state(states, wm, li);
 			mode = Ln.mode;
 			tbits = Ln.tbits;
 			q_in = Ln.q_in;
+			skip = Ln.skip;
 		}
-		if (mode == kGenerate)
+		if (mode == kGenerate || skip)
 			return false;
 		const uint32_t bytes = 8u << tbits;
 		mbar_expect_tx(&ps.bars[b], bytes);
@@ -621,17 +628,18 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 	for (int it = 0; w < total; w += gridDim.x, it++)
 	{
 		const int b = it & 1;
-		const int li = static_cast<int>(w / per);
-		const unsigned int r = static_cast<unsigned int>(w % per);
+		unsigned int r, items;
+		const int li = wm_find(wm, w, r, items);
 		if (li != ps.lc.li)
 		{
 			__syncthreads();
-			load_lattice_cache(states[li], li);
-			load_class_table(states[li]);
+			load_lattice_cache(wm_state(states, wm, li), li);
+			load_class_table(wm_state(states, wm, li));
 			__syncthreads();
 		}
 		const int mode = ps.lc.mode;
 		const long long wn = w + gridDim.x;
+		const long long lat_end = w - r + items; // first item of the next lattice
 		if (tid == 0 && wn < total)
 		{
 			// Buffer b ^ 1 may still be the source of the previous tile's q'
@@ -643,6 +651,8 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 			else
 				inflight1 = issue(wn, 1);
 		}
+		if (ps.lc.skip)
+			continue; // a finished session: no copy was issued for it
 		bool timed_out = false;
 		if (mode != kGenerate)
 		{
@@ -688,7 +698,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 		{
 			if (tid == 0)
 			{
-				atomicExch(&states[li].error, kErrTimeout);
+				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
 				if (b ? inflight0 : inflight1)
 					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
 				bulk_wait_all();
@@ -704,9 +714,9 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 		// Count this CTA's finished items of the lattice when it moves on to
 		// another lattice or runs out of work; the CTA completing the
 		// lattice runs its epilogue.
-		if (wn >= total || static_cast<int>(wn / per) != li)
+		if (wn >= total || wn >= lat_end)
 		{
-			LatticeDev &L = states[li];
+			LatticeDev &L = wm_state(states, wm, li);
 			__syncthreads();
 			if (tid == 0)
 			{
@@ -716,7 +726,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, i
 				bulk_wait_all(); // this lattice's q' stores are complete
 				__threadfence();
 				ps.last = atomicAdd(&L.k1_count, static_cast<unsigned int>(done)) ==
-						  static_cast<unsigned int>(per - done);
+						  items - static_cast<unsigned int>(done);
 			}
 			done = 0;
 			__syncthreads();
@@ -839,7 +849,7 @@ __device__ unsigned int multinomial_select(LatticeDev &L)
 // K2 epilogue of lattice L: the winning experiment (the block winners' argmin
 // for k = 1, the multinomial scoring for k >= 2) and, in session mode,
 // classification, the drawn response and the queued update.
-__device__ void k2_epilogue(LatticeDev &L, int per)
+__device__ void k2_epilogue(LatticeDev &L, unsigned int per)
 {
 	u64 bs = ~0ull;
 	unsigned int be = 0xFFFFFFFFu;
@@ -850,7 +860,7 @@ __device__ void k2_epilogue(LatticeDev &L, int per)
 	}
 	else
 	{
-		for (int i = threadIdx.x; i < per; i += kThreads)
+		for (unsigned int i = threadIdx.x; i < per; i += kThreads)
 		{
 			const u64 s2 = __ldcg(L.blk_score + i);
 			const unsigned int e2 = __ldcg(L.blk_e + i);
@@ -872,7 +882,8 @@ __device__ void k2_epilogue(LatticeDev &L, int per)
 		{
 			// Session stage (bgt::Lattice order: select -> update -> classify):
 			// classify the posterior the previous update produced, then queue
-			// this stage's update.
+			// this stage's update.  A stopping session ends once every atom
+			// is classified, and then leaves both passes idle (skip).
 			const int st = L.stage;
 			if (st > 0)
 			{
@@ -882,7 +893,9 @@ __device__ void k2_epilogue(LatticeDev &L, int per)
 				if (L.out_neg)
 					L.out_neg[st - 1] = L.neg;
 			}
-			if (st < L.stages)
+			const unsigned int all_atoms = L.atoms >= 32 ? 0xFFFFFFFFu : ((1u << L.atoms) - 1u);
+			const bool settled = L.sess_stop && st > 0 && (L.pos | L.neg) == all_atoms;
+			if (st < L.stages && !settled)
 			{
 				const unsigned int rsp = bgt_session_sample_response(L.dilution, L.n, L.k, be, L.truth, L.alpha, L.hpar,
 																	 L.seed, L.session, static_cast<uint32_t>(st));
@@ -898,6 +911,17 @@ __device__ void k2_epilogue(LatticeDev &L, int per)
 			else
 			{
 				L.sess_active = 0;
+				if (L.sess_stop)
+					L.skip = 1;
+			}
+			if (L.status)
+			{
+				SessionStatus *o = L.status;
+				o->stage = static_cast<unsigned int>(L.stage);
+				o->pos = L.pos;
+				o->neg = L.neg;
+				o->error = L.error;
+				o->running = static_cast<unsigned int>(L.sess_active);
 			}
 		}
 		L.k2_count = 0;
@@ -906,14 +930,14 @@ __device__ void k2_epilogue(LatticeDev &L, int per)
 }
 
 // K2: one W-column block of M1 (all 2^h rows, contiguous) per work item.
-__global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *states, int count, int per)
+__global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *states, WorkMap wm)
 {
 	u64 *const inbuf0 = tile_u64(0);
 	u64 *const inbuf1 = tile_u64(1);
 	u64 *const work = work_tile();
 	int *const shift = g_shift;
 	const unsigned int tid = threadIdx.x;
-	const long long total = static_cast<long long>(count) * per;
+	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
 		return;
@@ -926,8 +950,8 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	}
 	__syncthreads();
 	auto issue = [&](long long item, int b) -> bool {
-		const int li = static_cast<int>(item / per);
-		const unsigned int blk = static_cast<unsigned int>(item % per);
+		unsigned int blk, bcount;
+		const int li = wm_find(wm, item, blk, bcount);
 		int skip, hbits, colw, mbits;
 		u64 *src;
 		if (li == ps.lc.li)
@@ -940,7 +964,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		}
 		else
 		{
-			const LatticeDev &Ln = states[li];
+			const LatticeDev &Ln = wm_state(states, wm, li);
 			skip = Ln.skip;
 			hbits = Ln.hbits;
 			colw = Ln.colw;
@@ -963,12 +987,12 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	for (int it = 0; w < total; w += gridDim.x, it++)
 	{
 		const int b = it & 1;
-		const int li = static_cast<int>(w / per);
-		const unsigned int blk = static_cast<unsigned int>(w % per);
+		unsigned int blk, per;
+		const int li = wm_find(wm, w, blk, per);
 		if (li != ps.lc.li)
 		{
 			__syncthreads();
-			const LatticeDev &Lc = states[li];
+			const LatticeDev &Lc = wm_state(states, wm, li);
 			load_lattice_cache(Lc, li);
 			const int s_g = Lc.s_g;
 			// Rows of K1's partial sums carry tile scales; the middle pass's
@@ -1039,7 +1063,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		{
 			if (tid == 0)
 			{
-				atomicExch(&states[li].error, kErrTimeout);
+				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
 				if (b ? inflight0 : inflight1)
 					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
 			}
@@ -1128,7 +1152,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			const unsigned int y = y0 + (best_j << 2);
 			best_e = ((y >> logw) << row_shift) | col_base | (y & wmask);
 		}
-		LatticeDev &L = states[li];
+		LatticeDev &L = wm_state(states, wm, li);
 		// Singleton (atom) masses live in block 0 and in the blocks whose
 		// first column is a power of two.
 		if (want_masses)
@@ -1149,14 +1173,14 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			L.blk_e[blk] = best_e;
 		}
 		done++;
-		if (wn >= total || static_cast<int>(wn / per) != li)
+		if (wn >= total || wn >= w - blk + per)
 		{
 			__syncthreads();
 			if (tid == 0)
 			{
 				__threadfence();
 				ps.last = atomicAdd(&L.k2_count, static_cast<unsigned int>(done)) ==
-						  static_cast<unsigned int>(per - done);
+						  per - static_cast<unsigned int>(done);
 			}
 			done = 0;
 			__syncthreads();
@@ -1176,13 +1200,13 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 // scale, the zeta runs over the low mbits bits of the tile index (block
 // index bits 2 .. 2 + mbits), and the values are written transposed,
 // [column block][r_lo][r_hi][4], so that K2's blocks stay contiguous.
-__global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, int count, int per)
+__global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, WorkMap wm)
 {
 	u64 *const inbuf0 = tile_u64(0);
 	u64 *const inbuf1 = tile_u64(1);
 	u64 *const work = work_tile();
 	const unsigned int tid = threadIdx.x;
-	const long long total = static_cast<long long>(count) * per;
+	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
 		return;
@@ -1195,8 +1219,8 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, int
 	}
 	__syncthreads();
 	auto issue = [&](long long item, int b) -> bool {
-		const LatticeDev &Ln = states[item / per];
-		const unsigned int i = static_cast<unsigned int>(item % per);
+		unsigned int i, icount;
+		const LatticeDev &Ln = wm_state(states, wm, wm_find(wm, item, i, icount));
 		mbar_expect_tx(&ps.bars[b], kTileElems * 8u);
 		bulk_load(b ? inbuf1 : inbuf0, Ln.m1 + static_cast<size_t>(i) * kTileElems, kTileElems * 8u, &ps.bars[b]);
 		return true;
@@ -1208,12 +1232,12 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, int
 	for (int it = 0; w < total; w += gridDim.x, it++)
 	{
 		const int b = it & 1;
-		const int li = static_cast<int>(w / per);
-		const unsigned int item = static_cast<unsigned int>(w % per);
+		unsigned int item, items;
+		const int li = wm_find(wm, w, item, items);
 		if (li != ps.lc.li)
 		{
 			__syncthreads();
-			load_lattice_cache(states[li], li);
+			load_lattice_cache(wm_state(states, wm, li), li);
 			__syncthreads();
 		}
 		const long long wn = w + gridDim.x;
@@ -1265,7 +1289,7 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, int
 		{
 			if (tid == 0)
 			{
-				atomicExch(&states[li].error, kErrTimeout);
+				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
 				if (b ? inflight0 : inflight1)
 					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
 			}
@@ -1315,19 +1339,9 @@ __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo
 	const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
 	const unsigned int nlo = 1u << tbits, nhi = 1u << (atoms - tbits);
 	if (i < nlo)
-	{
-		double p = 1.0;
-		for (int a = 0; a < tbits; a++)
-			p *= (i & (1u << a)) ? (1.0 - pi0[a]) : pi0[a];
-		lo[i] = p;
-	}
+		lo[i] = prior_product(pi0, 0, tbits, i);
 	if (i < nhi)
-	{
-		double p = 1.0;
-		for (int a = tbits; a < atoms; a++)
-			p *= (i & (1u << (a - tbits))) ? (1.0 - pi0[a]) : pi0[a];
-		hi[i] = p;
-	}
+		hi[i] = prior_product(pi0, tbits, atoms - tbits, i);
 }
 
 // Exact fixed-point upset mass sum_{s superset of e} q[s] at the lattice's

@@ -69,6 +69,17 @@ enum K1Mode : int
 	kGenerate = 2 // q_out = prior_hi[row] * prior_lo[col]
 };
 
+// Host-visible progress of a device-driven session (mapped pinned memory),
+// written by the selection pass after every stage.
+struct SessionStatus
+{
+	unsigned int stage;   // stages run (selections made and applied or pending)
+	unsigned int running; // 0 once the session has ended
+	unsigned int pos, neg;
+	int error;
+	unsigned int pad[3];
+};
+
 struct LatticeDev
 {
 	// ---- geometry (host-set) ----
@@ -119,7 +130,57 @@ struct LatticeDev
 	unsigned long long seed, session;
 	unsigned int truth;
 	unsigned int *out_e, *out_r, *out_pos, *out_neg;
+	int sess_stop;                 // end once every atom is classified (else run all stages)
+	SessionStatus *status;         // optional progress record
 };
+
+// Work items of a batched launch.  Lattice li owns the items
+// [li * per, (li + 1) * per) when per > 0, else [prefix[li], prefix[li + 1])
+// (lattices of different sizes in one launch); slot maps li to its entry of
+// the state array (nullptr: entry li).
+struct WorkMap
+{
+	int count;
+	int per;
+	const unsigned int *prefix;
+	const int *slot;
+};
+
+__device__ __forceinline__ long long wm_total(const WorkMap &m)
+{
+	return m.per > 0 ? static_cast<long long>(m.count) * m.per : static_cast<long long>(__ldg(m.prefix + m.count));
+}
+
+// Lattice of item w; `item` is its index within the lattice and `items` the
+// lattice's item count.
+__device__ __forceinline__ int wm_find(const WorkMap &m, long long w, unsigned int &item, unsigned int &items)
+{
+	if (m.per > 0)
+	{
+		const int li = static_cast<int>(w / m.per);
+		item = static_cast<unsigned int>(w - static_cast<long long>(li) * m.per);
+		items = static_cast<unsigned int>(m.per);
+		return li;
+	}
+	int lo = 0, hi = m.count - 1; // the last li with prefix[li] <= w
+	while (lo < hi)
+	{
+		const int mid = (lo + hi + 1) >> 1;
+		if (static_cast<long long>(__ldg(m.prefix + mid)) <= w)
+			lo = mid;
+		else
+			hi = mid - 1;
+	}
+	const unsigned int p0 = __ldg(m.prefix + lo);
+	item = static_cast<unsigned int>(w - p0);
+	items = __ldg(m.prefix + lo + 1) - p0;
+	return lo;
+}
+
+__device__ __forceinline__ LatticeDev &wm_state(LatticeDev *states, const WorkMap &m, int li)
+{
+	return states[m.slot ? __ldg(m.slot + li) : li];
+}
 
 enum LatticeError : int
 {
@@ -130,6 +191,18 @@ enum LatticeError : int
 };
 
 // ------------------------------------------------------------------ helpers
+
+// Product prior of the `count` atoms from `first` for index bits i
+// (bit 1 = negative: 1 - pi0), in atom order; the posterior's prior is
+// prior_hi[s >> tbits] * prior_lo[s & (2^tbits - 1)]
+// (lattice_base.cpp:184-208 multiplies the same factors per state).
+__device__ __forceinline__ double prior_product(const double *pi0, int first, int count, unsigned int i)
+{
+	double p = 1.0;
+	for (int a = 0; a < count; a++)
+		p *= (i & (1u << a)) ? (1.0 - pi0[first + a]) : pi0[first + a];
+	return p;
+}
 
 __device__ __forceinline__ unsigned int tile_swz(unsigned int x) { return x ^ ((x >> 4) & 15u); }
 

@@ -31,8 +31,8 @@
 namespace bgt_gpu
 {
 
-__global__ void k1_zeta_low(LatticeDev *states, int count, int per);
-__global__ void k2_zeta_high_select(LatticeDev *states, int count, int per);
+__global__ void k1_zeta_low(LatticeDev *states, WorkMap wm);
+__global__ void k2_zeta_high_select(LatticeDev *states, WorkMap wm);
 
 namespace
 {
@@ -210,9 +210,10 @@ extern "C" int bgt_gpu_select_noalloc(const double *posterior, int subjects, int
 		LatticeDev *state = reinterpret_cast<LatticeDev *>(scratch);
 		const int sms = sm_count();
 		const int per1 = 1 << g.hbits;
-		k1_zeta_low<<<per1 < sms ? per1 : sms, kThreads, k1_smem_bytes(), s>>>(state, 1, per1);
+		k1_zeta_low<<<per1 < sms ? per1 : sms, kThreads, k1_smem_bytes(), s>>>(state, WorkMap{1, per1, nullptr, nullptr});
 		cuda_check(cudaGetLastError(), "noalloc k1 launch");
-		k2_zeta_high_select<<<g.nblk < sms ? g.nblk : sms, kThreads, k2_smem_bytes(g.hbits), s>>>(state, 1, g.nblk);
+		k2_zeta_high_select<<<g.nblk < sms ? g.nblk : sms, kThreads, k2_smem_bytes(g.hbits), s>>>(
+			state, WorkMap{1, g.nblk, nullptr, nullptr});
 		cuda_check(cudaGetLastError(), "noalloc k2 launch");
 		count_launches(2);
 		noalloc_finish<<<1, 32, 0, s>>>(experiment);

@@ -11,6 +11,7 @@ namespace bgt_gpu
 {
 
 struct LatticeDev;
+struct WorkMap;
 
 // A CUDA call failed or a kernel reported an error; mapped to status 4 at the
 // C ABI (the reference's BGT_CUDA_CHECK, include/bgt/detail/cuda_checks.hpp).
@@ -28,10 +29,21 @@ void set_error(const std::string &message);
 void count_launches(uint64_t n);
 void cuda_check(cudaError_t err, const char *what);
 void configure_kernels();
-LatticeGeometry make_geometry(int n, int k);
+// Tile and block shapes.  K2 blocks hold at most 16 columns by default, so
+// that one lattice spreads over many CTAs; `wide` fills each block to a full
+// tile instead (batched launches, where the parallelism comes from the number
+// of lattices).
+LatticeGeometry make_geometry(int n, int k, bool wide = false);
+// The dilution response table DilutionTable(n, alpha, h) flattened as
+// [(L - 1) * (n + 1) + r] (dilution.cpp:10-26).
+void dilution_rows(int n, double alpha, double h, double *flat);
 int check_supported(int subjects, int variants, int dilution, std::string *why);
 void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
 void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
+// Batched launches over lattices of different sizes (no middle pass); `items`
+// is the map's total work items.
+void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream);
+void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream);
 size_t k1_smem_bytes();
 size_t k2_smem_bytes(int hbits);
 int sm_count();

@@ -1,0 +1,650 @@
+// Served sessions: continuous batching of device-driven adaptive sessions.
+//
+// Every resident session is one LatticeDev slot.  A round advances all of
+// them by one stage with two batched launches over lattices of mixed sizes:
+// the update + low-bit zeta pass (K1, WorkMap with per-lattice tile counts)
+// and the high-bit zeta + selection pass (K2, per-lattice block counts),
+// whose epilogue classifies, samples the response and queues the next
+// update.  Sessions report progress through a status record in mapped pinned
+// host memory, so retiring them needs no copy.  Device memory comes from one
+// arena of the configured budget, carved per session by a first-fit
+// allocator; admission is first come first served.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "bgt_gpu.h"
+#include "bgt_serve.h"
+#include "lattice_kernels.cuh"
+#include "provider_internal.h"
+
+namespace bgt_gpu
+{
+namespace
+{
+
+constexpr int kServeMaxSubjects = 24; // tile + high passes only (no middle pass)
+constexpr int kMaxAdmitPerRound = 1024;
+constexpr size_t kAlign = 256;
+
+size_t align_up(size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
+
+// One admitted session's set-up: its state image (device pointers already
+// bound to its arena block), prior and dilution table.
+struct AdmitRecord
+{
+	LatticeDev image;
+	int slot;
+	int dil_len;
+	double pi0[kServeMaxSubjects];
+	double dil[kServeMaxSubjects * (kServeMaxSubjects + 1)];
+};
+
+// Writes each admitted session's prior tables and dilution table into its
+// arena block and its state into its slot (one CTA per session).
+__global__ void serve_admit(const AdmitRecord *recs, LatticeDev *states)
+{
+	const AdmitRecord &a = recs[blockIdx.x];
+	const LatticeDev &img = a.image;
+	const int tbits = img.tbits, hbits = img.hbits;
+	double *lo = const_cast<double *>(img.prior_lo);
+	double *hi = const_cast<double *>(img.prior_hi);
+	for (unsigned int i = threadIdx.x; i < (1u << tbits); i += blockDim.x)
+		lo[i] = prior_product(a.pi0, 0, tbits, i);
+	for (unsigned int i = threadIdx.x; i < (1u << hbits); i += blockDim.x)
+		hi[i] = prior_product(a.pi0, tbits, hbits, i);
+	double *dil = const_cast<double *>(img.dil);
+	for (int i = threadIdx.x; i < a.dil_len; i += blockDim.x)
+		dil[i] = a.dil[i];
+	static_assert(sizeof(LatticeDev) % 8 == 0, "state copied as 8-byte words");
+	const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&img);
+	unsigned long long *dst = reinterpret_cast<unsigned long long *>(states + a.slot);
+	for (unsigned int i = threadIdx.x; i < sizeof(LatticeDev) / 8; i += blockDim.x)
+		dst[i] = src[i];
+}
+
+// Byte layout of one session's arena block.
+struct SessionLayout
+{
+	size_t q, m1, tile_total, tile_scale, blk_score, blk_e, prior_lo, prior_hi, dil, bytes;
+};
+
+SessionLayout layout_for(const LatticeGeometry &g)
+{
+	SessionLayout s{};
+	const size_t states = size_t{1} << g.atoms;
+	const size_t rows = size_t{1} << g.hbits;
+	size_t off = 0;
+	auto take = [&](size_t bytes) {
+		const size_t at = off;
+		off += align_up(bytes);
+		return at;
+	};
+	s.q = take(states * sizeof(double));
+	s.m1 = take(states * sizeof(unsigned long long));
+	s.tile_total = take(rows * sizeof(unsigned long long));
+	s.tile_scale = take(rows * sizeof(int));
+	s.blk_score = take(static_cast<size_t>(g.nblk) * sizeof(unsigned long long));
+	s.blk_e = take(static_cast<size_t>(g.nblk) * sizeof(unsigned int));
+	s.prior_lo = take((size_t{1} << g.tbits) * sizeof(double));
+	s.prior_hi = take(rows * sizeof(double));
+	s.dil = take(static_cast<size_t>(g.n) * (g.n + 1) * sizeof(double));
+	s.bytes = off;
+	return s;
+}
+
+// First-fit allocator over the arena, coalescing on free.
+class Arena
+{
+  public:
+	void reset(size_t size)
+	{
+		free_.clear();
+		if (size)
+			free_[0] = size;
+	}
+	bool alloc(size_t bytes, size_t *offset)
+	{
+		for (auto it = free_.begin(); it != free_.end(); ++it)
+		{
+			if (it->second >= bytes)
+			{
+				*offset = it->first;
+				const size_t rest = it->second - bytes;
+				const size_t at = it->first + bytes;
+				free_.erase(it);
+				if (rest)
+					free_[at] = rest;
+				return true;
+			}
+		}
+		return false;
+	}
+	void release(size_t offset, size_t bytes)
+	{
+		auto it = free_.emplace(offset, bytes).first;
+		auto next = std::next(it);
+		if (next != free_.end() && it->first + it->second == next->first)
+		{
+			it->second += next->second;
+			free_.erase(next);
+		}
+		if (it != free_.begin())
+		{
+			auto prev = std::prev(it);
+			if (prev->first + prev->second == it->first)
+			{
+				prev->second += it->second;
+				free_.erase(it);
+			}
+		}
+	}
+
+  private:
+	std::map<size_t, size_t> free_;
+};
+
+struct Pending
+{
+	uint64_t ticket;
+	bgt_serve_request req;
+	std::vector<double> prior;
+	double submit_s;
+};
+
+struct Resident
+{
+	bool used = false;
+	Pending p;
+	LatticeGeometry g;
+	size_t arena_off = 0, arena_bytes = 0;
+	double admit_s = 0.0;
+	int rounds = 0;
+};
+
+struct Finished
+{
+	bgt_serve_result r;
+	std::vector<uint32_t> out; // [4][stages]
+};
+
+struct RoundLog
+{
+	double launch_s, done_s;
+	int sessions;
+};
+
+} // namespace
+} // namespace bgt_gpu
+
+using namespace bgt_gpu;
+
+struct bgt_gpu_server
+{
+	bgt_serve_config cfg{};
+	cudaStream_t stream = nullptr;
+	char *arena_dev = nullptr;
+	Arena arena;
+	LatticeDev *states = nullptr;
+	// Pinned, mapped: per slot 4 * max_stages outputs and a status record.
+	unsigned int *out_host = nullptr;
+	SessionStatus *status_host = nullptr;
+	unsigned int *out_dev = nullptr;
+	SessionStatus *status_dev = nullptr;
+	// Per round: admit records and the lattice list (slots, K1 and K2 prefixes).
+	AdmitRecord *admit_host = nullptr;
+	AdmitRecord *admit_dev = nullptr;
+	unsigned int *list_host = nullptr;
+	unsigned int *list_dev = nullptr;
+	std::vector<int> free_slots;
+	std::vector<Resident> slots;
+	std::deque<Pending> queue;
+	std::vector<int> round_slots; // slots of the round in flight
+	bool in_flight = false;
+	double launch_s = 0.0;
+	std::vector<RoundLog> rounds;
+	std::unordered_map<uint64_t, Finished> finished;
+	uint64_t next_ticket = 1;
+	std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+
+	double now() const
+	{
+		return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+	}
+
+	~bgt_gpu_server()
+	{
+		if (stream)
+			cudaStreamSynchronize(stream);
+		cudaFree(arena_dev);
+		cudaFree(states);
+		cudaFree(admit_dev);
+		cudaFree(list_dev);
+		cudaFreeHost(out_host);
+		cudaFreeHost(status_host);
+		cudaFreeHost(admit_host);
+		cudaFreeHost(list_host);
+		if (stream)
+			cudaStreamDestroy(stream);
+	}
+
+	unsigned int *outputs(int slot) { return out_host + static_cast<size_t>(slot) * 4 * cfg.max_stages; }
+
+	void retire(int slot, int error)
+	{
+		Resident &rs = slots[static_cast<size_t>(slot)];
+		const SessionStatus &st = status_host[slot];
+		Finished f{};
+		f.r.ticket = rs.p.ticket;
+		f.r.subjects = rs.g.n;
+		f.r.stages = static_cast<int>(std::min<unsigned int>(st.stage, static_cast<unsigned int>(cfg.max_stages)));
+		f.r.error = error;
+		f.r.positive_mask = st.pos;
+		f.r.negative_mask = st.neg;
+		f.r.submit_s = rs.p.submit_s;
+		f.r.admit_s = rs.admit_s;
+		f.r.finish_s = now();
+		f.r.rounds = rs.rounds;
+		const size_t S = static_cast<size_t>(cfg.max_stages);
+		const size_t n = static_cast<size_t>(f.r.stages);
+		f.out.resize(4 * n);
+		const unsigned int *o = outputs(slot);
+		for (size_t a = 0; a < 4; a++)
+			std::memcpy(f.out.data() + a * n, o + a * S, n * sizeof(uint32_t));
+		finished.emplace(rs.p.ticket, std::move(f));
+		arena.release(rs.arena_off, rs.arena_bytes);
+		rs.used = false;
+		rs.p.prior.clear();
+		free_slots.push_back(slot);
+	}
+
+	// Waits for the round in flight and retires the sessions it ended.
+	int complete_round()
+	{
+		if (!in_flight)
+			return 0;
+		cuda_check(cudaStreamSynchronize(stream), "round sync");
+		in_flight = false;
+		rounds.push_back(RoundLog{launch_s, now(), static_cast<int>(round_slots.size())});
+		int retired = 0;
+		bool stalled = false;
+		for (int slot : round_slots)
+		{
+			Resident &rs = slots[static_cast<size_t>(slot)];
+			rs.rounds++;
+			const SessionStatus &st = status_host[slot];
+			// A running session has made exactly one selection per round.
+			if (st.error == 0 && st.running && st.stage != static_cast<unsigned int>(rs.rounds))
+				stalled = true;
+		}
+		for (int slot : round_slots)
+		{
+			const SessionStatus &st = status_host[slot];
+			if (stalled || st.error != 0)
+			{
+				retire(slot, BGT_GPU_RUNTIME_FAILURE);
+				retired++;
+			}
+			else if (!st.running)
+			{
+				retire(slot, BGT_GPU_OK);
+				retired++;
+			}
+		}
+		round_slots.clear();
+		if (stalled)
+			throw CudaFailure("a served round did not advance every session (a bounded wait expired)");
+		return retired;
+	}
+
+	// Admits queued sessions while a slot and arena space are free; returns
+	// the number of admit records written.
+	int admit()
+	{
+		int count = 0;
+		while (!queue.empty() && !free_slots.empty() && count < kMaxAdmitPerRound)
+		{
+			Pending &p = queue.front();
+			const LatticeGeometry g = make_geometry(p.req.subjects, 1, true);
+			const SessionLayout lay = layout_for(g);
+			size_t off = 0;
+			if (!arena.alloc(lay.bytes, &off))
+				break; // first come first served: wait for memory
+			const int slot = free_slots.back();
+			free_slots.pop_back();
+			Resident &rs = slots[static_cast<size_t>(slot)];
+			rs.used = true;
+			rs.g = g;
+			rs.arena_off = off;
+			rs.arena_bytes = lay.bytes;
+			rs.admit_s = now();
+			rs.rounds = 0;
+			rs.p = std::move(p);
+			queue.pop_front();
+			char *base = arena_dev + off;
+			AdmitRecord &a = admit_host[count++];
+			std::memset(&a, 0, sizeof(a));
+			LatticeDev &h = a.image;
+			const bgt_serve_request &rq = rs.p.req;
+			h.n = g.n;
+			h.k = 1;
+			h.atoms = g.atoms;
+			h.tbits = g.tbits;
+			h.hbits = g.hbits;
+			h.nblk = g.nblk;
+			h.colw = g.colw;
+			h.logw = g.logw;
+			h.mbits = 0;
+			h.dilution = rq.dilution;
+			h.orig_n = g.n;
+			h.q_in = reinterpret_cast<const double *>(base + lay.q);
+			h.q_out = reinterpret_cast<double *>(base + lay.q);
+			h.m1 = reinterpret_cast<unsigned long long *>(base + lay.m1);
+			h.m2 = nullptr;
+			h.tile_total = reinterpret_cast<unsigned long long *>(base + lay.tile_total);
+			h.tile_scale = reinterpret_cast<int *>(base + lay.tile_scale);
+			h.blk_score = reinterpret_cast<unsigned long long *>(base + lay.blk_score);
+			h.blk_e = reinterpret_cast<unsigned int *>(base + lay.blk_e);
+			h.dil = reinterpret_cast<const double *>(base + lay.dil);
+			h.prior_lo = reinterpret_cast<const double *>(base + lay.prior_lo);
+			h.prior_hi = reinterpret_cast<const double *>(base + lay.prior_hi);
+			h.ftab = nullptr;
+			h.mode = kGenerate;
+			h.z_norm = 1.0;
+			h.active = g.n >= 32 ? 0xFFFFFFFFu : ((1u << g.n) - 1u);
+			h.masses_in_k2 = 1;
+			h.sess_active = 1;
+			h.stage = 0;
+			h.stages = cfg.max_stages;
+			h.alpha = rq.alpha;
+			h.hpar = rq.h;
+			h.up = cfg.threshold_up;
+			h.lo = cfg.threshold_lo;
+			h.seed = rq.seed;
+			h.session = rq.session;
+			h.truth = rq.true_state;
+			const size_t S = static_cast<size_t>(cfg.max_stages);
+			unsigned int *o = out_dev + static_cast<size_t>(slot) * 4 * S;
+			h.out_e = o;
+			h.out_r = o + S;
+			h.out_pos = o + 2 * S;
+			h.out_neg = o + 3 * S;
+			h.sess_stop = 1;
+			h.status = status_dev + slot;
+			a.slot = slot;
+			std::copy(rs.p.prior.begin(), rs.p.prior.end(), a.pi0);
+			a.dil_len = 0;
+			if (rq.dilution)
+			{
+				dilution_rows(g.n, rq.alpha, rq.h, a.dil);
+				a.dil_len = g.n * (g.n + 1);
+			}
+		}
+		return count;
+	}
+
+	// Launches one round over every resident session.
+	void launch(int admitted)
+	{
+		launch_s = now();
+		if (admitted > 0)
+		{
+			cuda_check(cudaMemcpyAsync(admit_dev, admit_host, static_cast<size_t>(admitted) * sizeof(AdmitRecord),
+									   cudaMemcpyHostToDevice, stream),
+					   "admit upload");
+			serve_admit<<<admitted, 256, 0, stream>>>(admit_dev, states);
+			cuda_check(cudaGetLastError(), "admit launch");
+			count_launches(1);
+		}
+		round_slots.clear();
+		for (int s = 0; s < cfg.max_sessions; s++)
+			if (slots[static_cast<size_t>(s)].used)
+				round_slots.push_back(s);
+		const int count = static_cast<int>(round_slots.size());
+		if (count == 0)
+			return;
+		const size_t M = static_cast<size_t>(cfg.max_sessions);
+		int *slot_list = reinterpret_cast<int *>(list_host);
+		unsigned int *p1 = list_host + M;
+		unsigned int *p2 = list_host + 2 * M + 1;
+		unsigned int t1 = 0, t2 = 0;
+		for (int i = 0; i < count; i++)
+		{
+			const Resident &rs = slots[static_cast<size_t>(round_slots[static_cast<size_t>(i)])];
+			slot_list[i] = round_slots[static_cast<size_t>(i)];
+			p1[i] = t1;
+			p2[i] = t2;
+			t1 += 1u << rs.g.hbits;
+			t2 += static_cast<unsigned int>(rs.g.nblk);
+		}
+		p1[count] = t1;
+		p2[count] = t2;
+		cuda_check(cudaMemcpyAsync(list_dev, list_host, (3 * M + 2) * sizeof(unsigned int), cudaMemcpyHostToDevice,
+								   stream),
+				   "round list upload");
+		const int *d_slots = reinterpret_cast<const int *>(list_dev);
+		const WorkMap w1{count, 0, list_dev + M, d_slots};
+		const WorkMap w2{count, 0, list_dev + 2 * M + 1, d_slots};
+		launch_k1_map(states, w1, t1, stream);
+		launch_k2_map(states, w2, t2, stream);
+		in_flight = true;
+	}
+};
+
+namespace
+{
+
+template <typename F>
+int server_guarded(F &&f)
+{
+	try
+	{
+		return f();
+	}
+	catch (const CudaFailure &ex)
+	{
+		set_error(ex.what());
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+	catch (const std::bad_alloc &)
+	{
+		set_error("host allocation failed");
+		return BGT_GPU_RUNTIME_FAILURE;
+	}
+}
+
+} // namespace
+
+extern "C" {
+
+int bgt_gpu_server_create(const bgt_serve_config *config, bgt_gpu_server **out)
+{
+	if (!config || !out)
+	{
+		set_error("null config or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	*out = nullptr;
+	if (config->max_sessions < 1 || config->max_stages < 1 || config->memory_budget == 0)
+	{
+		set_error("max_sessions, max_stages and memory_budget must be positive");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	int devices = 0;
+	if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
+	{
+		cudaGetLastError();
+		set_error("no CUDA device");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return server_guarded([&]() -> int {
+		configure_kernels();
+		std::unique_ptr<bgt_gpu_server> s(new bgt_gpu_server());
+		s->cfg = *config;
+		const size_t M = static_cast<size_t>(config->max_sessions);
+		const size_t S = static_cast<size_t>(config->max_stages);
+		cuda_check(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "stream create");
+		if (cudaMalloc(&s->arena_dev, config->memory_budget) != cudaSuccess)
+		{
+			cudaGetLastError();
+			set_error("the memory budget could not be allocated on the device");
+			return BGT_GPU_UNSUPPORTED;
+		}
+		s->arena.reset(config->memory_budget);
+		cuda_check(cudaMalloc(&s->states, M * sizeof(LatticeDev)), "alloc slots");
+		cuda_check(cudaMemset(s->states, 0, M * sizeof(LatticeDev)), "clear slots");
+		cuda_check(cudaHostAlloc(&s->out_host, M * 4 * S * sizeof(unsigned int), cudaHostAllocMapped),
+				   "alloc pinned outputs");
+		cuda_check(cudaHostAlloc(&s->status_host, M * sizeof(SessionStatus), cudaHostAllocMapped),
+				   "alloc pinned status");
+		std::memset(s->status_host, 0, M * sizeof(SessionStatus));
+		cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->out_dev), s->out_host, 0),
+				   "map pinned outputs");
+		cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s->status_dev), s->status_host, 0),
+				   "map pinned status");
+		const size_t admit_cap = std::min<size_t>(M, kMaxAdmitPerRound);
+		cuda_check(cudaHostAlloc(&s->admit_host, admit_cap * sizeof(AdmitRecord), cudaHostAllocDefault),
+				   "alloc admit staging");
+		cuda_check(cudaMalloc(&s->admit_dev, admit_cap * sizeof(AdmitRecord)), "alloc admit records");
+		cuda_check(cudaHostAlloc(&s->list_host, (3 * M + 2) * sizeof(unsigned int), cudaHostAllocDefault),
+				   "alloc round list staging");
+		cuda_check(cudaMalloc(&s->list_dev, (3 * M + 2) * sizeof(unsigned int)), "alloc round list");
+		s->slots.resize(M);
+		for (int i = static_cast<int>(M) - 1; i >= 0; i--)
+			s->free_slots.push_back(i);
+		*out = s.release();
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_server_destroy(bgt_gpu_server *server)
+{
+	delete server;
+	return BGT_GPU_OK;
+}
+
+int bgt_gpu_server_submit(bgt_gpu_server *server, const bgt_serve_request *request, uint64_t *ticket)
+{
+	if (!server || !request || !request->prior)
+	{
+		set_error("null server, request or prior");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (request->subjects < 1 || request->subjects > kServeMaxSubjects)
+	{
+		set_error("served sessions have 1 to 24 subjects");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (request->dilution != 0 && request->dilution != 1)
+	{
+		set_error("dilution must be 0 or 1");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (request->selector < 0 || request->selector > 2)
+	{
+		set_error("unsupported selector");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	const LatticeGeometry g = make_geometry(request->subjects, 1, true);
+	if (layout_for(g).bytes > server->cfg.memory_budget)
+	{
+		set_error("the session is larger than the server's memory budget");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return server_guarded([&]() -> int {
+		Pending p;
+		p.ticket = server->next_ticket++;
+		p.req = *request;
+		p.prior.assign(request->prior, request->prior + request->subjects);
+		p.req.prior = nullptr;
+		p.submit_s = server->now();
+		if (ticket)
+			*ticket = p.ticket;
+		server->queue.push_back(std::move(p));
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_server_step(bgt_gpu_server *server, int *active, int *queued, int *finished)
+{
+	if (!server)
+	{
+		set_error("null server");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	return server_guarded([&]() -> int {
+		const int retired = server->complete_round();
+		const int admitted = server->admit();
+		server->launch(admitted);
+		if (active)
+			*active = server->in_flight ? static_cast<int>(server->round_slots.size()) : 0;
+		if (queued)
+			*queued = static_cast<int>(server->queue.size());
+		if (finished)
+			*finished = retired;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_server_result(bgt_gpu_server *server, uint64_t ticket, bgt_serve_result *result, uint32_t *experiments,
+						  uint32_t *responses, uint32_t *positive_masks, uint32_t *negative_masks, int capacity)
+{
+	if (!server)
+	{
+		set_error("null server");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	auto it = server->finished.find(ticket);
+	if (it == server->finished.end())
+	{
+		set_error("unknown ticket or session still running");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	const Finished &f = it->second;
+	if (result)
+		*result = f.r;
+	const size_t n = static_cast<size_t>(f.r.stages);
+	const size_t m = std::min<size_t>(n, static_cast<size_t>(capacity > 0 ? capacity : 0));
+	uint32_t *dst[4] = {experiments, responses, positive_masks, negative_masks};
+	for (size_t a = 0; a < 4; a++)
+		if (dst[a] && m)
+			std::memcpy(dst[a], f.out.data() + a * n, m * sizeof(uint32_t));
+	return BGT_GPU_OK;
+}
+
+int bgt_gpu_server_rounds(bgt_gpu_server *server, int first, int count, double *launch_s, double *done_s,
+						  int *sessions, int *total)
+{
+	if (!server)
+	{
+		set_error("null server");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	const int n = static_cast<int>(server->rounds.size());
+	if (total)
+		*total = n;
+	for (int i = 0; i < count; i++)
+	{
+		const int r = first + i;
+		if (r < 0 || r >= n)
+			break;
+		const RoundLog &lg = server->rounds[static_cast<size_t>(r)];
+		if (launch_s)
+			launch_s[i] = lg.launch_s;
+		if (done_s)
+			done_s[i] = lg.done_s;
+		if (sessions)
+			sessions[i] = lg.sessions;
+	}
+	return BGT_GPU_OK;
+}
+
+} // extern "C"

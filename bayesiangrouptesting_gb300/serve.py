@@ -1,0 +1,158 @@
+"""Served adaptive-testing sessions (continuous batching) over the C ABI of
+include/bgt_serve.h.
+
+``Server`` keeps many sessions resident on the GPU and advances all of them
+by one select -> update -> classify stage per round, in two batched launches
+whatever the mix of sizes.  ``submit`` queues a request; ``step`` waits for
+the round in flight, retires finished sessions, admits queued ones that fit
+the memory budget and launches the next round without waiting for it.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from ._native import ServeConfigC, ServeRequestC, ServeResultC, load
+from .api import _call
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_up = ctypes.POINTER(ctypes.c_uint32)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+@dataclass
+class SessionRequest:
+    """One adaptive session: binary subjects, internal subject order."""
+
+    subjects: int
+    prior: np.ndarray
+    true_state: int
+    seed: int
+    session: int
+    dilution: bool = False
+    alpha: float = 0.99
+    h: float = 0.005
+    selector: int = 0  # 0 auto (Op-BHA), 1 Op-BHA, 2 Op-BBPA
+
+
+@dataclass
+class SessionResult:
+    ticket: int
+    subjects: int
+    stages: int
+    error: int
+    pos: int
+    neg: int
+    submit_s: float
+    admit_s: float
+    finish_s: float
+    rounds: int
+    experiments: np.ndarray
+    responses: np.ndarray
+    pos_masks: np.ndarray
+    neg_masks: np.ndarray
+
+
+def session_bytes(subjects: int) -> int:
+    """Device bytes one served session holds (posterior + zeta partial sums
+    + tables), as the server counts them against its budget."""
+    # Mirrors the layout of serve.cu: each buffer rounded up to 256 bytes.
+    def up(b):
+        return (b + 255) // 256 * 256
+
+    tbits = min(subjects, 13)
+    hbits = subjects - tbits
+    w = max(4, 8192 >> hbits)
+    w = min(w, 1 << tbits)
+    nblk = (1 << tbits) // w
+    states, rows = 1 << subjects, 1 << hbits
+    return (up(8 * states) * 2 + up(8 * rows) + up(4 * rows) + up(8 * nblk) + up(4 * nblk) + up(8 << tbits)
+            + up(8 * rows) + up(8 * subjects * (subjects + 1)))
+
+
+class Server:
+    def __init__(self, memory_budget: int, max_sessions: int = 4096, max_stages: int = 40,
+                 threshold_up: float = 0.01, threshold_lo: float = 0.01):
+        self._lib = load()
+        self.max_stages = max_stages
+        cfg = ServeConfigC(memory_budget, max_sessions, max_stages, threshold_up, threshold_lo)
+        self._handle = ctypes.c_void_p()
+        _call(self._lib.bgt_gpu_server_create(ctypes.byref(cfg), ctypes.byref(self._handle)))
+        self._keep: Dict[int, np.ndarray] = {}
+
+    def close(self) -> None:
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            self._lib.bgt_gpu_server_destroy(h)
+            self._handle = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, req: SessionRequest) -> int:
+        prior = np.ascontiguousarray(req.prior, dtype=np.float64)
+        if prior.size != req.subjects:
+            raise ValueError("prior length must equal subjects")
+        c = ServeRequestC(1 if req.dilution else 0, req.subjects, prior.ctypes.data_as(_dp), req.alpha, req.h,
+                          req.selector, req.seed, req.session, req.true_state)
+        ticket = ctypes.c_uint64()
+        _call(self._lib.bgt_gpu_server_submit(self._handle, ctypes.byref(c), ctypes.byref(ticket)))
+        return int(ticket.value)
+
+    def step(self):
+        """One round; returns (active, queued, finished)."""
+        a, q, f = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _call(self._lib.bgt_gpu_server_step(self._handle, ctypes.byref(a), ctypes.byref(q), ctypes.byref(f)))
+        return a.value, q.value, f.value
+
+    def run_until_idle(self, max_rounds: int = 1_000_000) -> int:
+        """Steps until nothing is resident or queued; returns the rounds run."""
+        rounds = 0
+        while rounds < max_rounds:
+            active, queued, _ = self.step()
+            if active == 0 and queued == 0:
+                return rounds
+            rounds += 1
+        raise RuntimeError("server did not drain")
+
+    def result(self, ticket: int) -> Optional[SessionResult]:
+        r = ServeResultC()
+        S = self.max_stages
+        arrays = [np.zeros(S, np.uint32) for _ in range(4)]
+        status = self._lib.bgt_gpu_server_result(self._handle, ticket, ctypes.byref(r),
+                                                 *[a.ctypes.data_as(_up) for a in arrays], S)
+        if status != 0:
+            return None
+        n = r.stages
+        return SessionResult(int(r.ticket), r.subjects, n, r.error, int(r.positive_mask), int(r.negative_mask),
+                             r.submit_s, r.admit_s, r.finish_s, r.rounds, *[a[:n] for a in arrays])
+
+    def rounds(self):
+        """Completed rounds: arrays of launch and completion times (seconds
+        since the server was created) and sessions per round."""
+        total = ctypes.c_int()
+        _call(self._lib.bgt_gpu_server_rounds(self._handle, 0, 0, None, None, None, ctypes.byref(total)))
+        n = total.value
+        ls, ds, ss = np.zeros(n), np.zeros(n), np.zeros(n, np.int32)
+        _call(self._lib.bgt_gpu_server_rounds(self._handle, 0, n, ls.ctypes.data_as(_dp), ds.ctypes.data_as(_dp),
+                                              ss.ctypes.data_as(_ip), ctypes.byref(total)))
+        return ls, ds, ss
+
+
+def serve_all(requests: List[SessionRequest], memory_budget: int, max_sessions: int = 4096,
+              max_stages: int = 40, threshold_up: float = 0.01, threshold_lo: float = 0.01):
+    """Submits every request at once, drains the server and returns the
+    results in request order."""
+    with Server(memory_budget, max_sessions, max_stages, threshold_up, threshold_lo) as srv:
+        tickets = [srv.submit(r) for r in requests]
+        srv.run_until_idle()
+        return [srv.result(t) for t in tickets]

@@ -166,6 +166,20 @@ BGT_GPU_API int bgt_gpu_session_run(bgt_gpu_lattice *lattice, int selector, int 
 									uint32_t true_state, uint32_t *experiments, uint32_t *responses,
 									uint32_t *positive_masks, uint32_t *negative_masks);
 
+/* The same session, ending after the first stage whose classification
+ * covers every atom (or after max_stages stages): the served-session loop
+ * "select -> update -> classify until classified".  *stages_run receives the
+ * number of stages run; the output arrays (max_stages entries each) are
+ * written for those stages.  No reference counterpart: the reference has no
+ * session driver; this is the one-session-at-a-time loop that the server
+ * (bgt_serve.h) batches. */
+BGT_GPU_API int bgt_gpu_session_run_until_classified(bgt_gpu_lattice *lattice, int selector, int max_stages,
+													 double alpha, double h, double threshold_up,
+													 double threshold_lo, uint64_t seed, uint64_t session,
+													 uint32_t true_state, uint32_t *experiments, uint32_t *responses,
+													 uint32_t *positive_masks, uint32_t *negative_masks,
+													 int *stages_run);
+
 /* Kernel timing for benchmarks: while enabled, every launch of the two
  * lattice passes is bracketed by CUDA events on its stream.
  * bgt_gpu_profile_read synchronises and reports, per pass (index 0: the

@@ -1,0 +1,103 @@
+/* Served adaptive-testing sessions on one GB300: continuous batching.
+ *
+ * A server keeps many independent sessions' posteriors resident in device
+ * memory and advances all of them by one stage per round
+ * (select -> response -> update -> classify, the order of
+ * bgt_gpu_session_run_until_classified), with every session of the round,
+ * whatever its size, in the same two batched launches.  Requests are queued
+ * on submit and admitted, first come first served, as slots and memory free
+ * up: a session needs about 16 * 2^n bytes (posterior and zeta partial sums)
+ * plus its tables, counted against the configured budget.  A session ends
+ * when every subject is classified or after max_stages stages, and is retired
+ * at the next round.
+ *
+ * No reference counterpart: the reference has no serving layer.  Sessions are
+ * binary (one variant), 1 to 24 subjects, FP64; the responses come from the
+ * per-session streams of bgt_session_rng.h, so a served session's
+ * experiments, responses and masks equal those of the same session run alone
+ * (bgt_gpu_session_run_until_classified).
+ *
+ * Threading: a server and its calls belong to one host thread.  All device
+ * work runs on the server's own stream. */
+#ifndef BGT_SERVE_H
+#define BGT_SERVE_H
+
+#include <stdint.h>
+
+#include "bgt_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct bgt_gpu_server bgt_gpu_server;
+
+typedef struct bgt_serve_config
+{
+	uint64_t memory_budget; /* device bytes for session state, allocated once at create */
+	int max_sessions;       /* resident sessions at most */
+	int max_stages;         /* stage cap per session (>= 1) */
+	double threshold_up;    /* classification thresholds (update_classification) */
+	double threshold_lo;
+} bgt_serve_config;
+
+typedef struct bgt_serve_request
+{
+	int dilution;        /* 0: non-dilution, 1: dilution (DilutionTable(subjects, alpha, h)) */
+	int subjects;        /* 1 .. 24 */
+	const double *prior; /* per-subject prior infection probabilities, copied at submit */
+	double alpha, h;     /* response model parameters */
+	int selector;        /* 0 auto (Op-BHA), 1 Op-BHA, 2 Op-BBPA */
+	uint64_t seed, session;
+	uint32_t true_state; /* internal subject order */
+} bgt_serve_request;
+
+typedef struct bgt_serve_result
+{
+	uint64_t ticket;
+	int subjects;
+	int stages;              /* stages run */
+	int error;               /* 0, or the BGT_GPU_* status of a failed session */
+	uint32_t positive_mask;  /* final classification (internal order) */
+	uint32_t negative_mask;
+	double submit_s, admit_s, finish_s; /* host clock, seconds since the server was created */
+	int rounds;              /* rounds the session was resident for */
+} bgt_serve_result;
+
+/* Creates a server: allocates the memory budget, the state slots and the
+ * pinned result areas.  Status 2 when the budget cannot be allocated or no
+ * device is present. */
+BGT_GPU_API int bgt_gpu_server_create(const bgt_serve_config *config, bgt_gpu_server **out);
+BGT_GPU_API int bgt_gpu_server_destroy(bgt_gpu_server *server);
+
+/* Queues a session; *ticket identifies it.  Status 2 for an unsupported
+ * request (subjects outside 1..24, a session larger than the whole budget). */
+BGT_GPU_API int bgt_gpu_server_submit(bgt_gpu_server *server, const bgt_serve_request *request,
+									  uint64_t *ticket);
+
+/* One round.  Waits for the round in flight, retires the sessions it ended,
+ * admits queued sessions that fit, and launches the next round without
+ * waiting for it, so the caller can queue more requests meanwhile.  Outputs
+ * (any may be null): sessions in the launched round, sessions still queued,
+ * sessions retired by this call.  With nothing resident or admissible it
+ * launches nothing and *active is 0. */
+BGT_GPU_API int bgt_gpu_server_step(bgt_gpu_server *server, int *active, int *queued, int *finished);
+
+/* A retired session's record and its per-stage outputs (capacity entries
+ * each, any array may be null).  Status 2 while the ticket is unknown or
+ * not yet retired. */
+BGT_GPU_API int bgt_gpu_server_result(bgt_gpu_server *server, uint64_t ticket, bgt_serve_result *result,
+									  uint32_t *experiments, uint32_t *responses, uint32_t *positive_masks,
+									  uint32_t *negative_masks, int capacity);
+
+/* Rounds completed so far; with non-null arrays, copies rounds
+ * [first, first + count): host launch and completion times (seconds since
+ * create) and the sessions in each round. */
+BGT_GPU_API int bgt_gpu_server_rounds(bgt_gpu_server *server, int first, int count, double *launch_s, double *done_s,
+									  int *sessions, int *total);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,127 @@
+"""Served sessions (continuous batching, include/bgt_serve.h): each session's
+result is the same alone, in a mix of sizes and types, under admission
+pressure and with requests arriving while rounds run, and equals the
+one-session device loop and the oracle's session (truncated where the
+session is fully classified)."""
+import numpy as np
+import pytest
+
+import bayesiangrouptesting_gb300 as bgt
+from bayesiangrouptesting_gb300.serve import Server, SessionRequest, serve_all, session_bytes
+
+pytestmark = pytest.mark.gpu
+
+MAX_STAGES = 40
+GB = 1 << 30
+
+
+def _requests(count, seed, n_lo=8, n_hi=16):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        n = int(rng.integers(n_lo, n_hi + 1))
+        pi0 = rng.uniform(0.005, 0.15, n)
+        truth = 0
+        for j in range(n):
+            if rng.random() >= pi0[j]:
+                truth |= 1 << j  # internal bit 1 = negative
+        dil = bool(rng.integers(0, 2))
+        reqs.append(SessionRequest(n, pi0, truth, seed=seed, session=i, dilution=dil,
+                                   alpha=0.01 if dil else 0.99, h=0.005))
+    return reqs
+
+
+def _same(a, b):
+    assert a.error == 0 and b.error == 0
+    assert a.stages == b.stages
+    for key in ("experiments", "responses", "pos_masks", "neg_masks"):
+        np.testing.assert_array_equal(getattr(a, key), getattr(b, key))
+    assert (a.pos, a.neg) == (b.pos, b.neg)
+
+
+def _settled_prefix(n, pos, neg, max_stages):
+    full = (1 << n) - 1
+    for i in range(len(pos)):
+        if (int(pos[i]) | int(neg[i])) == full:
+            return i + 1
+    return max_stages
+
+
+def test_served_mix_equals_alone_and_plain_loop(gpu):
+    reqs = _requests(48, seed=41)
+    mixed = serve_all(reqs, memory_budget=2 * GB)
+    assert all(r is not None and r.error == 0 for r in mixed)
+    for i in (0, 5, 17, 31, 47):
+        alone = serve_all([reqs[i]], memory_budget=GB)[0]
+        _same(mixed[i], alone)
+        q = reqs[i]
+        t = bgt.LatticeType.replicated_dilution if q.dilution else bgt.LatticeType.replicated_non_dilution
+        lat = bgt.Lattice(t, q.subjects, q.prior)
+        plain = lat.run_session_until_classified(MAX_STAGES, q.true_state, seed=q.seed, session=q.session,
+                                                 selector=bgt.SelectorType.auto_select, alpha=q.alpha, h=q.h)
+        assert plain["stages"] == mixed[i].stages
+        np.testing.assert_array_equal(plain["experiments"], mixed[i].experiments)
+        np.testing.assert_array_equal(plain["responses"], mixed[i].responses)
+        np.testing.assert_array_equal(plain["pos"], mixed[i].pos_masks)
+        np.testing.assert_array_equal(plain["neg"], mixed[i].neg_masks)
+
+
+def test_served_sessions_match_oracle(gpu, oracle):
+    reqs = _requests(12, seed=77, n_lo=4, n_hi=12)
+    got = serve_all(reqs, memory_budget=GB)
+    for q, r in zip(reqs, got):
+        want = oracle.session(1 if q.dilution else 0, q.subjects, 1, q.prior, MAX_STAGES, q.seed, q.session,
+                              q.true_state, selector=0, alpha=q.alpha, h=q.h)
+        stop = _settled_prefix(q.subjects, want["pos"], want["neg"], MAX_STAGES)
+        assert r.stages == stop
+        np.testing.assert_array_equal(r.experiments, want["experiments"][:stop])
+        np.testing.assert_array_equal(r.responses, want["responses"][:stop])
+        np.testing.assert_array_equal(r.pos_masks, want["pos"][:stop])
+        np.testing.assert_array_equal(r.neg_masks, want["neg"][:stop])
+
+
+def test_admission_under_memory_and_slot_limits(gpu):
+    reqs = _requests(10, seed=5, n_lo=12, n_hi=12)
+    free = serve_all(reqs, memory_budget=GB)
+    budget = 3 * session_bytes(12) + 4096
+    with Server(budget, max_sessions=8) as srv:
+        tickets = [srv.submit(r) for r in reqs]
+        active, queued, _ = srv.step()
+        assert active == 3 and queued == 7  # three sessions fit the budget
+        srv.run_until_idle()
+        tight = [srv.result(t) for t in tickets]
+    for a, b in zip(free, tight):
+        _same(a, b)
+    with Server(GB, max_sessions=2) as srv:
+        tickets = [srv.submit(r) for r in reqs]
+        active, queued, _ = srv.step()
+        assert active == 2 and queued == 8
+        srv.run_until_idle()
+        for a, t in zip(free, tickets):
+            _same(a, srv.result(t))
+
+
+def test_requests_arriving_while_rounds_run(gpu):
+    reqs = _requests(30, seed=9, n_lo=6, n_hi=18)
+    ref = serve_all(reqs, memory_budget=2 * GB)
+    with Server(2 * GB) as srv:
+        tickets = []
+        for i, r in enumerate(reqs):
+            tickets.append(srv.submit(r))
+            if i % 3 == 2:
+                srv.step()  # the round runs while the next requests are queued
+        srv.run_until_idle()
+        late = [srv.result(t) for t in tickets]
+        launch, done, sessions = srv.rounds()
+        assert len(launch) > 0 and np.all(done >= launch) and sessions.max() > 1
+    for a, b in zip(ref, late):
+        _same(a, b)
+        assert b.submit_s <= b.admit_s <= b.finish_s
+
+
+def test_rejects_unsupported_requests(gpu):
+    with Server(GB // 4) as srv:
+        with pytest.raises(bgt.Error):
+            srv.submit(SessionRequest(25, np.full(25, 0.1), 0, 1, 1))
+        with pytest.raises(bgt.Error):
+            srv.submit(SessionRequest(24, np.full(24, 0.1), 0, 1, 1))  # 256 MB + > budget
