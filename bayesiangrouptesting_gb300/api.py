@@ -341,6 +341,16 @@ class Lattice:
         _call(self._lib.bgt_gpu_lattice_atom_masses(self._handle, out.ctypes.data_as(_dp)))
         return out
 
+    def reset(self, prior) -> None:
+        """Back to the product prior of `prior` (same shape), reusing the
+        device buffers (bgt_gpu_lattice_reset)."""
+        prior = np.ascontiguousarray(prior, dtype=np.float64)
+        if prior.size != self._subjects * self._variants:
+            raise ValueError("prior length must equal subjects * variants.")
+        self._prior = prior
+        _call(self._lib.bgt_gpu_lattice_reset(self._handle, prior.ctypes.data_as(_dp)))
+        self._pos = self._neg = 0
+
     # -- session -------------------------------------------------------------
     def select_experiment(self, selector: SelectorType = SelectorType.auto_select) -> int:
         out = ctypes.c_uint32()

@@ -48,6 +48,16 @@ WORKLOAD = "binary dilution lattice n=24 (2^24 FP64 states), 32-stage Op-BBPA se
 
 M64 = (1 << 64) - 1
 
+# Served workload: sessions of n ~ U{8..22} binary subjects, half dilution
+# (alpha 0.01, h 0.005), priors U[0.005, 0.15], true state from the prior,
+# select -> update -> classify until classified or 40 stages, Poisson arrivals,
+# admitted against a 150 GB device budget.
+SERVE_SESSIONS = 4096
+SERVE_STAGES = 40
+SERVE_BUDGET = 150 << 30
+SERVE_RATE = 20000.0  # arrivals per second: well above the served throughput
+SERVE_SEED = 20261203
+
 
 # -------------------------------------------------- workload (host copies of
 # the counter-based streams of include/bgt_session_rng.h)
@@ -222,6 +232,111 @@ def run_reference(args, world, rank):
     return 0
 
 
+def serve_requests(seed: int, count: int):
+    from bayesiangrouptesting_gb300.serve import SessionRequest
+
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, count))
+    reqs = []
+    for i in range(count):
+        n = int(rng.integers(8, 23))
+        pi0 = rng.uniform(0.005, 0.15, n)
+        draws = rng.random(n)
+        truth = int(sum(1 << j for j in range(n) if draws[j] >= pi0[j]))  # bit 1 = negative
+        dil = bool(rng.random() < 0.5)
+        reqs.append(SessionRequest(n, pi0, truth, seed=seed, session=i, dilution=dil, alpha=ALPHA if dil else 0.99,
+                                   h=H, selector=0))
+    return reqs, arrivals
+
+
+def run_serving(count: int):
+    """Served sessions (continuous batching) against the plain loop that runs
+    the same sessions one at a time on the device.  Both are end to end:
+    priors come from host memory and results land in host memory."""
+    import bayesiangrouptesting_gb300 as bgt
+    from bayesiangrouptesting_gb300 import _native
+    from bayesiangrouptesting_gb300.serve import Server
+
+    reqs, arrivals = serve_requests(SERVE_SEED, count)
+    # Warm-up: a small served batch and one plain session per lattice shape.
+    warm, _ = serve_requests(SERVE_SEED + 1, 64)
+    with Server(8 << 30, max_sessions=64, max_stages=SERVE_STAGES) as srv:
+        for r in warm:
+            srv.submit(r)
+        srv.run_until_idle()
+    launches0 = _native.launches()
+    with Server(SERVE_BUDGET, max_sessions=count, max_stages=SERVE_STAGES, threshold_up=THRESHOLD,
+                threshold_lo=THRESHOLD) as srv:
+        tickets = [0] * count
+        nxt = 0
+        t0 = time.perf_counter()
+        while True:
+            now = time.perf_counter() - t0
+            while nxt < count and arrivals[nxt] <= now:
+                tickets[nxt] = srv.submit(reqs[nxt])
+                nxt += 1
+            active, queued, _ = srv.step()
+            if active == 0 and queued == 0:
+                if nxt == count:
+                    break
+                time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+        served_wall = time.perf_counter() - t0
+        served = [srv.result(t) for t in tickets]
+        launch, done, sessions = srv.rounds()
+    served_launches = _native.launches() - launches0
+    if any(r is None or r.error for r in served):
+        raise SystemExit("a served session failed")
+    stages = np.array([r.stages for r in served])
+    round_ms = 1e3 * (done - launch)
+    stage_lat = np.repeat(round_ms, sessions)
+    sess_lat = np.array([r.finish_s - r.submit_s for r in served]) * 1e3
+
+    # Plain loop: one session at a time through the device session loop, a
+    # lattice per (n, type) reused by reset.
+    lattices = {}
+    for q in reqs:
+        key = (q.subjects, q.dilution)
+        if key not in lattices:
+            t = bgt.LatticeType.replicated_dilution if q.dilution else bgt.LatticeType.replicated_non_dilution
+            lattices[key] = bgt.Lattice(t, q.subjects, q.prior)
+    for q in warm[:8]:
+        lat = lattices.get((q.subjects, q.dilution))
+        if lat is not None:
+            lat.reset(q.prior)
+            lat.run_session_until_classified(SERVE_STAGES, q.true_state, q.seed, q.session, alpha=q.alpha, h=q.h)
+    identical = True
+    plain_ms = np.zeros(count)
+    t0 = time.perf_counter()
+    for i, q in enumerate(reqs):
+        s0 = time.perf_counter()
+        lat = lattices[(q.subjects, q.dilution)]
+        lat.reset(q.prior)
+        out = lat.run_session_until_classified(SERVE_STAGES, q.true_state, q.seed, q.session, alpha=q.alpha, h=q.h,
+                                               threshold_up=THRESHOLD, threshold_lo=THRESHOLD)
+        plain_ms[i] = 1e3 * (time.perf_counter() - s0)
+        identical &= out["stages"] == served[i].stages and np.array_equal(out["experiments"], served[i].experiments)
+    plain_wall = time.perf_counter() - t0
+    lattices.clear()
+    total_stages = int(stages.sum())
+    plain_stage_lat = plain_ms / np.maximum(stages, 1)
+    return {
+        "workload": f"{count} sessions, n ~ U{{8..22}} binary, half dilution (alpha {ALPHA}, h {H}), "
+                    f"pi0 ~ U[0.005, 0.15], until classified or {SERVE_STAGES} stages, Poisson arrivals "
+                    f"{SERVE_RATE:.0f}/s, {SERVE_BUDGET >> 30} GB budget, FP64",
+        "sessions_per_s": count / served_wall, "session_stages_per_s": total_stages / served_wall,
+        "wall_s": served_wall, "rounds": int(len(launch)), "mean_sessions_per_round": float(sessions.mean()),
+        "stage_latency_ms": {"p50": float(np.percentile(stage_lat, 50)), "p99": float(np.percentile(stage_lat, 99))},
+        "session_latency_ms": {"p50": float(np.percentile(sess_lat, 50)), "p99": float(np.percentile(sess_lat, 99))},
+        "stages_per_session": float(stages.mean()), "gpu_launches": int(served_launches),
+        "plain_loop": {"sessions_per_s": count / plain_wall, "session_stages_per_s": total_stages / plain_wall,
+                       "wall_s": plain_wall,
+                       "stage_latency_ms": {"p50": float(np.percentile(plain_stage_lat, 50)),
+                                            "p99": float(np.percentile(plain_stage_lat, 99))}},
+        "speedup_vs_plain_loop": plain_wall / served_wall,
+        "identical_to_plain_loop": bool(identical),
+    }
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -315,6 +430,11 @@ def run_gpu(args, world, rank, local):
         cv, cwall = cpu_baseline(stages=args.cpu_stages, workers=1)
         cpu = {"value": cv, "unit": "stages/s", "cores": 1, "kind": "port",
                "sample": f"one n=24 session, {args.cpu_stages} stages, oracle port on 1 core ({cwall:.1f} s)"}
+    serving = None
+    if rank == 0 and world == 1 and args.serve_sessions > 0:
+        with ClockSampler(local) as serve_clocks:
+            serving = run_serving(args.serve_sessions)
+        serving["clocks"] = serve_clocks.summary()
     line = {
         "metric": METRIC, "value": value, "unit": "stages/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
@@ -330,6 +450,7 @@ def run_gpu(args, world, rank, local):
         "cpu_baseline": cpu,
         "clocks": clocks.summary(),
         "gpu_launches": launches,
+        "serving": serving,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -348,6 +469,8 @@ def main():
     ap.add_argument("--cpu-stages", type=int, default=3, help="stages in the bounded CPU-baseline sample")
     ap.add_argument("--ref-stages", type=int, default=2, help="stages per core per step in the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-sessions", type=int, default=SERVE_SESSIONS,
+                    help="sessions in the served-workload measurement (0: skip it)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":
