@@ -41,6 +41,7 @@ class ServeConfigC(ctypes.Structure):
         ("max_stages", c_int),
         ("threshold_up", c_double),
         ("threshold_lo", c_double),
+        ("precision", c_int),
     ]
 
 
@@ -96,6 +97,7 @@ SIGNATURES = {
     "bgt_gpu_lattice_read_posterior": ([c_void_p, _dp], c_int),
     "bgt_gpu_lattice_posterior_probability": ([c_void_p, c_uint32, _dp], c_int),
     "bgt_gpu_lattice_upset_mass": ([c_void_p, c_uint32, _dp], c_int),
+    "bgt_gpu_lattice_max_abs_diff": ([c_void_p, c_void_p, _dp], c_int),
     "bgt_gpu_lattice_atom_masses": ([c_void_p, _dp], c_int),
     "bgt_gpu_session_run": ([c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_uint64, c_uint64,
                              c_uint32, _up, _up, _up, _up], c_int),

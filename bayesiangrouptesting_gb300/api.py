@@ -336,6 +336,13 @@ class Lattice:
         _call(self._lib.bgt_gpu_lattice_read_posterior(self._handle, out.ctypes.data_as(_dp)))
         return out
 
+    def max_abs_diff(self, other: "Lattice") -> float:
+        """max over states of |p_self(s) - p_other(s)| (normalised posteriors),
+        computed on the device."""
+        out = ctypes.c_double()
+        _call(self._lib.bgt_gpu_lattice_max_abs_diff(self._handle, other._handle, ctypes.byref(out)))
+        return out.value
+
     def atom_masses(self) -> np.ndarray:
         out = np.empty(self._subjects * self._variants)
         _call(self._lib.bgt_gpu_lattice_atom_masses(self._handle, out.ctypes.data_as(_dp)))

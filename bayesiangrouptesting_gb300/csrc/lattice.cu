@@ -26,6 +26,8 @@ namespace bgt_gpu
 __global__ void k1_zeta_low(LatticeDev *states, WorkMap wm);
 __global__ void k2_zeta_high_select(LatticeDev *states, WorkMap wm);
 __global__ void kmid_zeta(LatticeDev *states, WorkMap wm);
+__global__ void posterior_diff_kernel(const LatticeDev *a, const LatticeDev *b, unsigned long long states,
+									  unsigned long long *out);
 __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
 __global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, unsigned long long *out);
 
@@ -460,9 +462,14 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 		set_error("lattice type must be 0 (non-dilution) or 1 (dilution)");
 		return BGT_GPU_UNSUPPORTED;
 	}
-	if (precision != BGT_GPU_FP64)
+	if (precision != BGT_GPU_FP64 && precision != BGT_GPU_FP32)
 	{
-		set_error("only FP64 lattices are supported by this build");
+		set_error("precision must be BGT_GPU_FP64 or BGT_GPU_FP32");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (precision == BGT_GPU_FP32 && subjects * variants < 2)
+	{
+		set_error("FP32 lattices need at least 2 atoms (bulk copies move 16-byte multiples)");
 		return BGT_GPU_UNSUPPORTED;
 	}
 	if (!device_present())
@@ -484,7 +491,8 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			const size_t states = size_t{1} << g.atoms;
 			const size_t rows = size_t{1} << g.hbits;
 			cuda_check(cudaMalloc(&lat->dev, sizeof(LatticeDev)), "alloc state");
-			cuda_check(cudaMalloc(&lat->q, states * sizeof(double)), "alloc posterior");
+			const size_t esize = precision == BGT_GPU_FP32 ? sizeof(float) : sizeof(double);
+			cuda_check(cudaMalloc(&lat->q, states * esize), "alloc posterior");
 			cuda_check(cudaMalloc(&lat->m1, static_cast<size_t>(g.nblk) * rows * g.colw * sizeof(unsigned long long)),
 					   "alloc zeta partials");
 			cuda_check(cudaMalloc(&lat->tile_total, rows * sizeof(unsigned long long)), "alloc tile totals");
@@ -524,6 +532,7 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			h.mbits = g.mbits;
 			h.m2 = lat->m2;
 			h.masses_in_k2 = 1;
+			h.fp32 = precision == BGT_GPU_FP32 ? 1 : 0;
 			h.dilution = lattice_type;
 			h.orig_n = subjects;
 			h.q_in = lat->q;
@@ -749,6 +758,19 @@ int bgt_gpu_lattice_read_posterior(bgt_gpu_lattice *lattice, double *out)
 		if (lattice->update_pending || lattice->k1_pending)
 			lattice->run_k1();
 		const size_t states = size_t{1} << lattice->g.atoms;
+		if (lattice->precision == BGT_GPU_FP32)
+		{
+			// FP32 storage, widened to FP64 while normalising.
+			std::vector<float> tmp(states);
+			cuda_check(cudaMemcpyAsync(tmp.data(), lattice->q, states * sizeof(float), cudaMemcpyDeviceToHost,
+									   lattice->stream),
+					   "posterior read");
+			const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
+			lattice->check_device_error();
+			for (size_t s = 0; s < states; s++)
+				out[s] = static_cast<double>(tmp[s]) / z;
+			return BGT_GPU_OK;
+		}
 		cuda_check(cudaMemcpyAsync(out, lattice->q, states * sizeof(double), cudaMemcpyDeviceToHost, lattice->stream),
 				   "posterior read");
 		const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
@@ -776,10 +798,57 @@ int bgt_gpu_lattice_posterior_probability(bgt_gpu_lattice *lattice, uint32_t sta
 		if (lattice->update_pending || lattice->k1_pending)
 			lattice->run_k1();
 		double v = 0.0;
-		cuda_check(cudaMemcpyAsync(&v, lattice->q + state, sizeof(double), cudaMemcpyDeviceToHost, lattice->stream),
-				   "posterior read");
+		if (lattice->precision == BGT_GPU_FP32)
+		{
+			float f = 0.0f;
+			cuda_check(cudaMemcpyAsync(&f, reinterpret_cast<const float *>(lattice->q) + state, sizeof(float),
+									   cudaMemcpyDeviceToHost, lattice->stream),
+					   "posterior read");
+			cuda_check(cudaStreamSynchronize(lattice->stream), "posterior read sync");
+			v = f;
+		}
+		else
+		{
+			cuda_check(cudaMemcpyAsync(&v, lattice->q + state, sizeof(double), cudaMemcpyDeviceToHost,
+									   lattice->stream),
+					   "posterior read");
+		}
 		const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
 		*out = v / z;
+		return BGT_GPU_OK;
+	});
+}
+
+int bgt_gpu_lattice_max_abs_diff(bgt_gpu_lattice *a, bgt_gpu_lattice *b, double *out)
+{
+	if (!a || !b || !out)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (a->g.atoms != b->g.atoms)
+	{
+		set_error("the lattices have different shapes");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return guarded([&]() -> int {
+		for (bgt_gpu_lattice *l : {a, b})
+		{
+			if (l->update_pending || l->k1_pending)
+				l->run_k1();
+			cuda_check(cudaStreamSynchronize(l->stream), "lattice sync");
+			l->check_device_error();
+		}
+		cuda_check(cudaMemsetAsync(a->scratch_u64, 0, sizeof(unsigned long long), a->stream), "memset");
+		posterior_diff_kernel<<<4 * sm_count(), 256, 0, a->stream>>>(a->dev, b->dev, 1ull << a->g.atoms,
+																		a->scratch_u64);
+		cuda_check(cudaGetLastError(), "posterior diff launch");
+		count_launches(1);
+		unsigned long long bits = 0;
+		cuda_check(cudaMemcpyAsync(&bits, a->scratch_u64, sizeof(bits), cudaMemcpyDeviceToHost, a->stream),
+				   "diff read");
+		cuda_check(cudaStreamSynchronize(a->stream), "diff sync");
+		std::memcpy(out, &bits, sizeof(double));
 		return BGT_GPU_OK;
 	});
 }

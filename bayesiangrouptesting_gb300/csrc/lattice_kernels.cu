@@ -146,7 +146,7 @@ __device__ __forceinline__ void argmin_block(u64 &s, unsigned int &e, u64 *ws, u
 struct LatCache
 {
 	int li;
-	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix, mbits;
+	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix, mbits, fp32;
 	unsigned int e, active;
 	const double *q_in;
 	double *q_out;
@@ -168,6 +168,7 @@ struct PipeShared
 	uint64_t bars[2];
 	LatCache lc;
 	double ctab[kMaxClasses];
+	float ctab32[kMaxClasses]; // the same factors for FP32 lattices
 	float fred[32];
 	u64 ws[32];
 	u64 wsh[32];
@@ -315,7 +316,46 @@ struct ItemCfg
 	int tbits, hbits, colw, logw;
 	int dilution_classes; // 1: class = popcount(e & s); 0: class = contained
 	double c_in, c_out;   // non-dilution update factors (contained / not)
+	float c_in32, c_out32; // the same for FP32 lattices
 	int k, n, radix;      // k >= 2: mixed-radix classes into g_ctab
+};
+
+// Update factors in the lattice's storage type.
+template <typename T>
+__device__ __forceinline__ T class_factor(int c)
+{
+	if constexpr (sizeof(T) == 4)
+		return ps.ctab32[c];
+	else
+		return ps.ctab[c];
+}
+template <typename T>
+__device__ __forceinline__ T multinomial_factor(int idx)
+{
+	if constexpr (sizeof(T) == 4)
+		return reinterpret_cast<const float *>(g_ctab)[idx];
+	else
+		return g_ctab[idx];
+}
+template <typename T>
+__device__ __forceinline__ T contained_factor(const ItemCfg &cfg, bool in)
+{
+	if constexpr (sizeof(T) == 4)
+		return in ? cfg.c_in32 : cfg.c_out32;
+	else
+		return in ? cfg.c_in : cfg.c_out;
+}
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<double>
+{
+	typedef double2 type;
+};
+template <>
+struct Vec2<float>
+{
+	typedef float2 type;
 };
 
 // Mixed-radix likelihood class of state s for a multinomial update.
@@ -334,70 +374,73 @@ __device__ __forceinline__ int multinomial_class(const ItemCfg &cfg, unsigned in
 }
 
 // One K1 work item (tile r of lattice L), specialised on the K1 mode.
-template <int kMode>
+template <int kMode, typename T>
 __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int b, bool abort, u64 &total_out,
 										int &scale_out)
 {
-	double *const in = tile_f64(b);
+	typedef typename Vec2<T>::type V2;
+	T *const in = reinterpret_cast<T *>(tile_f64(b));
 	u64 *const work = work_tile();
 	const unsigned int tid = threadIdx.x;
 	const int tbits = cfg.tbits;
 	const unsigned int tsize = 1u << tbits;
 	const unsigned int e = cfg.e;
 	const size_t base = static_cast<size_t>(r) << tbits;
-	double *q_out = cfg.q_out;
+	T *q_out = reinterpret_cast<T *>(cfg.q_out);
 	const double phi = cfg.phi;
-	(void)q_out;
 	// Phase A: pairs (x, x + 1) with x = map_a(tid, 2 i); register bits
 	// {0, 10, 11, 12}.  Reads the tile from the bulk-copied buffer (or the
 	// prior tables), applies the update, writes q'.
-	double v[kPerThread];
+	T v[kPerThread];
 	float f = 0.0f;
-	int hmax = 0;
+	bool bad = false;
 #pragma unroll
 	for (int i = 0; i < kPerThread / 2; i++)
 	{
 		const unsigned int x = map_a(tid, 2 * i);
-		double2 p = make_double2(0.0, 0.0);
+		V2 p;
+		p.x = T(0);
+		p.y = T(0);
 		if (x < tsize)
 		{
 			if (kMode == kGenerate)
 			{
 				const double2 lo = *reinterpret_cast<const double2 *>(cfg.prior_lo + x);
-				p = make_double2(phi * lo.x, phi * lo.y);
+				p.x = static_cast<T>(phi * lo.x);
+				p.y = static_cast<T>(phi * lo.y);
 			}
 			else
 			{
-				p = *reinterpret_cast<const double2 *>(in + x);
+				p = *reinterpret_cast<const V2 *>(in + x);
 			}
 			if (kMode == kUpdate)
 			{
 				const unsigned int s0 = static_cast<unsigned int>(base) | x;
 				if (cfg.k > 1)
 				{
-					p.x *= g_ctab[multinomial_class(cfg, s0)];
-					p.y *= g_ctab[multinomial_class(cfg, s0 | 1u)];
+					p.x *= multinomial_factor<T>(multinomial_class(cfg, s0));
+					p.y *= multinomial_factor<T>(multinomial_class(cfg, s0 | 1u));
 				}
 				else if (cfg.dilution_classes)
 				{
-					p.x *= ps.ctab[__popc(e & s0)];
-					p.y *= ps.ctab[__popc(e & (s0 | 1u))];
+					p.x *= class_factor<T>(__popc(e & s0));
+					p.y *= class_factor<T>(__popc(e & (s0 | 1u)));
 				}
 				else
 				{
-					p.x *= (e & s0) == e ? cfg.c_in : cfg.c_out;
-					p.y *= (e & (s0 | 1u)) == e ? cfg.c_in : cfg.c_out;
+					p.x *= contained_factor<T>(cfg, (e & s0) == e);
+					p.y *= contained_factor<T>(cfg, (e & (s0 | 1u)) == e);
 				}
 			}
 			if (kMode != kLoad)
-				*reinterpret_cast<double2 *>(in + x) = p; // q', bulk-stored by the caller
+				*reinterpret_cast<V2 *>(in + x) = p; // q', bulk-stored by the caller
 		}
 		v[2 * i] = p.x;
 		v[2 * i + 1] = p.y;
 		f += approx_scaled_hi(p.x) + approx_scaled_hi(p.y);
-		hmax = max(hmax, max(__double2hiint(p.x), __double2hiint(p.y)));
+		bad |= non_finite(p.x) | non_finite(p.y);
 	}
-	if (hmax >= 0x7FF00000)
+	if (bad)
 		ps.flag = 1;
 	if (kMode != kLoad)
 		proxy_fence(); // q' in shared memory -> visible to the bulk store
@@ -406,7 +449,7 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 		return true;
 	if (kMode != kLoad && threadIdx.x == 0)
 	{
-		bulk_store(q_out + base, in, static_cast<uint32_t>(sizeof(double)) << tbits);
+		bulk_store(q_out + base, in, static_cast<uint32_t>(sizeof(T)) << tbits);
 		bulk_commit();
 	}
 	// Scale so that the tile total lands in [2^61, 2^62 (1 + 2^-20)).
@@ -509,7 +552,10 @@ __device__ __forceinline__ void load_class_table(const LatticeDev &L)
 			const int pc = L.dilution ? c : (c ? pool : (pool > 0 ? pool - 1 : 0));
 			f *= binary_likelihood(L.dilution, pool, pc, (L.pend_r >> v) & 1u, L.dil, L.orig_n + 1);
 		}
-		g_ctab[idx] = f / z;
+		if (L.fp32)
+			reinterpret_cast<float *>(g_ctab)[idx] = static_cast<float>(f / z);
+		else
+			g_ctab[idx] = f / z;
 	}
 }
 
@@ -528,6 +574,7 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			ps.ctab[tid] = static_cast<int>(tid) <= pool
 							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1) / L.z_norm
 							   : 0.0;
+			ps.ctab32[tid] = static_cast<float>(ps.ctab[tid]);
 		}
 		__syncwarp();
 		if (tid == 0)
@@ -542,6 +589,7 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.logw = L.logw;
 			c.dilution = L.dilution;
 			c.skip = L.skip;
+			c.fp32 = L.fp32;
 			c.n = L.n;
 			c.k = k;
 			c.radix = radix;
@@ -596,7 +644,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 	auto issue = [&](long long item, int b) -> bool {
 		unsigned int rn, rcount;
 		const int li = wm_find(wm, item, rn, rcount);
-		int mode, tbits, skip;
+		int mode, tbits, skip, fp32;
 		const double *q_in;
 		if (li == ps.lc.li)
 		{
@@ -604,6 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 			tbits = ps.lc.tbits;
 			q_in = ps.lc.q_in;
 			skip = ps.lc.skip;
+			fp32 = ps.lc.fp32;
 		}
 		else
 		{
@@ -612,12 +661,14 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 			tbits = Ln.tbits;
 			q_in = Ln.q_in;
 			skip = Ln.skip;
+			fp32 = Ln.fp32;
 		}
 		if (mode == kGenerate || skip)
 			return false;
-		const uint32_t bytes = 8u << tbits;
+		const uint32_t bytes = (fp32 ? 4u : 8u) << tbits;
 		mbar_expect_tx(&ps.bars[b], bytes);
-		bulk_load(b ? inbuf1 : inbuf0, q_in + (static_cast<size_t>(rn) << tbits), bytes, &ps.bars[b]);
+		bulk_load(b ? inbuf1 : inbuf0, reinterpret_cast<const char *>(q_in) + static_cast<size_t>(rn) * bytes, bytes,
+				  &ps.bars[b]);
 		return true;
 	};
 	uint32_t parity0 = 0u, parity1 = 0u;
@@ -682,18 +733,32 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 		cfg.dilution_classes = ps.lc.dilution;
 		cfg.c_in = ps.lc.c_in;
 		cfg.c_out = ps.lc.c_out;
+		cfg.c_in32 = static_cast<float>(ps.lc.c_in);
+		cfg.c_out32 = static_cast<float>(ps.lc.c_out);
 		cfg.k = ps.lc.k;
 		cfg.n = ps.lc.n;
 		cfg.radix = ps.lc.radix;
 		u64 tile_total = 0;
 		int tile_scale = 0;
 		bool abort;
-		if (mode == kUpdate)
-			abort = k1_item<kUpdate>(cfg, r, b, timed_out, tile_total, tile_scale);
-		else if (mode == kGenerate)
-			abort = k1_item<kGenerate>(cfg, r, b, timed_out, tile_total, tile_scale);
+		if (ps.lc.fp32)
+		{
+			if (mode == kUpdate)
+				abort = k1_item<kUpdate, float>(cfg, r, b, timed_out, tile_total, tile_scale);
+			else if (mode == kGenerate)
+				abort = k1_item<kGenerate, float>(cfg, r, b, timed_out, tile_total, tile_scale);
+			else
+				abort = k1_item<kLoad, float>(cfg, r, b, timed_out, tile_total, tile_scale);
+		}
 		else
-			abort = k1_item<kLoad>(cfg, r, b, timed_out, tile_total, tile_scale);
+		{
+			if (mode == kUpdate)
+				abort = k1_item<kUpdate, double>(cfg, r, b, timed_out, tile_total, tile_scale);
+			else if (mode == kGenerate)
+				abort = k1_item<kGenerate, double>(cfg, r, b, timed_out, tile_total, tile_scale);
+			else
+				abort = k1_item<kLoad, double>(cfg, r, b, timed_out, tile_total, tile_scale);
+		}
 		if (abort)
 		{
 			if (tid == 0)
@@ -1366,12 +1431,36 @@ __global__ void upset_mass_kernel(const LatticeDev *state, unsigned int e, u64 *
 			jj >>= 1;
 			fb ^= low;
 		}
-		acc += to_fixed(L.q_in[s], L.s_g);
+		const double v = L.fp32 ? static_cast<double>(reinterpret_cast<const float *>(L.q_in)[s]) : L.q_in[s];
+		acc += to_fixed(v, L.s_g);
 	}
 	for (int o = 16; o > 0; o >>= 1)
 		acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
 	if ((threadIdx.x & 31) == 0)
 		atomicAdd(out, acc);
+}
+
+// max over states of |a_s / Z_a - b_s / Z_b| for two lattices of the same
+// shape, either storage type; `out` accumulates the maximum as the bit
+// pattern of a non-negative double (ordered like the value).
+__global__ void posterior_diff_kernel(const LatticeDev *a, const LatticeDev *b, unsigned long long states,
+									  unsigned long long *out)
+{
+	const double ia = 1.0 / a->z_norm, ib = 1.0 / b->z_norm;
+	const bool fa = a->fp32 != 0, fb = b->fp32 != 0;
+	const double *qa = a->q_in, *qb = b->q_in;
+	double m = 0.0;
+	for (unsigned long long s = blockIdx.x * static_cast<unsigned long long>(blockDim.x) + threadIdx.x; s < states;
+		 s += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+	{
+		const double va = fa ? static_cast<double>(reinterpret_cast<const float *>(qa)[s]) : qa[s];
+		const double vb = fb ? static_cast<double>(reinterpret_cast<const float *>(qb)[s]) : qb[s];
+		m = fmax(m, fabs(va * ia - vb * ib));
+	}
+	for (int o = 16; o > 0; o >>= 1)
+		m = fmax(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+	if ((threadIdx.x & 31) == 0)
+		atomicMax(out, static_cast<unsigned long long>(__double_as_longlong(m)));
 }
 
 } // namespace bgt_gpu

@@ -94,6 +94,7 @@ struct LatticeDev
 	int mbits;    // lattices above 24 atoms: tile-index bits transformed by the middle pass
 	int dilution; // 0 / 1
 	int orig_n;   // subjects of the dilution table
+	int fp32;     // posterior stored as FP32 (q_in / q_out then point to floats)
 	// ---- buffers (host-set) ----
 	const double *q_in;
 	double *q_out;
@@ -215,6 +216,14 @@ __device__ __forceinline__ float approx_scaled_hi(double v)
 	return d <= 0 ? 0.0f : __int_as_float(static_cast<int>(static_cast<unsigned int>(d) << 3));
 }
 
+// FP32-stored posterior value v * 2^64 as FP32 (exact: an exponent shift);
+// 0 for zero and subnormal v.
+__device__ __forceinline__ float approx_scaled_hi(float v)
+{
+	const int b = __float_as_int(v);
+	return (b >> 23) == 0 ? 0.0f : __int_as_float(b + (64 << 23));
+}
+
 // v * 2^64 truncated to FP32 (never above the true value); 0 when below the
 // FP32 normal range.  Integer-only: no FP64 conversion instruction.
 __device__ __forceinline__ float approx_scaled(double v)
@@ -260,6 +269,23 @@ __device__ __forceinline__ unsigned long long to_fixed_fast(double v, int scale)
 	rs = rs < 1 ? 1 : (rs > 64 ? 64 : rs);
 	return (((m << 11) >> (rs - 1)) + 1ull) >> 1;
 }
+
+// The same rounding for an FP32 value (24-bit significand placed at bit 63):
+// identical to to_fixed_fast of the value widened to FP64.
+__device__ __forceinline__ unsigned long long to_fixed_fast(float v, int scale)
+{
+	const unsigned int b = static_cast<unsigned int>(__float_as_int(v));
+	const int e = static_cast<int>(b >> 23);
+	const unsigned long long m = static_cast<unsigned long long>((b & 0x7FFFFFu) | (static_cast<unsigned int>(e != 0) << 23));
+	int rs = 190 - scale - (e > 1 ? e : 1);
+	rs = rs < 1 ? 1 : (rs > 64 ? 64 : rs);
+	return (((m << 40) >> (rs - 1)) + 1ull) >> 1;
+}
+
+// Non-finite (or, for the exponent test, huge) values trip the lattice's
+// error flag.
+__device__ __forceinline__ bool non_finite(double v) { return __double2hiint(v) >= 0x7FF00000; }
+__device__ __forceinline__ bool non_finite(float v) { return __float_as_int(v) >= 0x7F800000; }
 
 // round-half-up(v / 2^rs) for 0 <= rs <= 63 and v < 2^63, branch-free.
 __device__ __forceinline__ unsigned long long shr_round(unsigned long long v, int rs)

@@ -77,7 +77,7 @@ struct SessionLayout
 	size_t q, m1, tile_total, tile_scale, blk_score, blk_e, prior_lo, prior_hi, dil, bytes;
 };
 
-SessionLayout layout_for(const LatticeGeometry &g)
+SessionLayout layout_for(const LatticeGeometry &g, bool fp32)
 {
 	SessionLayout s{};
 	const size_t states = size_t{1} << g.atoms;
@@ -88,7 +88,7 @@ SessionLayout layout_for(const LatticeGeometry &g)
 		off += align_up(bytes);
 		return at;
 	};
-	s.q = take(states * sizeof(double));
+	s.q = take(states * (fp32 ? sizeof(float) : sizeof(double)));
 	s.m1 = take(states * sizeof(unsigned long long));
 	s.tile_total = take(rows * sizeof(unsigned long long));
 	s.tile_scale = take(rows * sizeof(int));
@@ -314,7 +314,7 @@ struct bgt_gpu_server
 		{
 			Pending &p = queue.front();
 			const LatticeGeometry g = make_geometry(p.req.subjects, 1, true);
-			const SessionLayout lay = layout_for(g);
+			const SessionLayout lay = layout_for(g, cfg.precision == BGT_GPU_FP32);
 			size_t off = 0;
 			if (!arena.alloc(lay.bytes, &off))
 				break; // first come first served: wait for memory
@@ -343,6 +343,7 @@ struct bgt_gpu_server
 			h.colw = g.colw;
 			h.logw = g.logw;
 			h.mbits = 0;
+			h.fp32 = cfg.precision == BGT_GPU_FP32 ? 1 : 0;
 			h.dilution = rq.dilution;
 			h.orig_n = g.n;
 			h.q_in = reinterpret_cast<const double *>(base + lay.q);
@@ -478,6 +479,11 @@ int bgt_gpu_server_create(const bgt_serve_config *config, bgt_gpu_server **out)
 		set_error("max_sessions, max_stages and memory_budget must be positive");
 		return BGT_GPU_UNSUPPORTED;
 	}
+	if (config->precision != BGT_GPU_FP64 && config->precision != BGT_GPU_FP32)
+	{
+		set_error("precision must be BGT_GPU_FP64 or BGT_GPU_FP32");
+		return BGT_GPU_UNSUPPORTED;
+	}
 	int devices = 0;
 	if (cudaGetDeviceCount(&devices) != cudaSuccess || devices == 0)
 	{
@@ -538,9 +544,10 @@ int bgt_gpu_server_submit(bgt_gpu_server *server, const bgt_serve_request *reque
 		set_error("null server, request or prior");
 		return BGT_GPU_MISSING_DILUTION;
 	}
-	if (request->subjects < 1 || request->subjects > kServeMaxSubjects)
+	const bool fp32 = server->cfg.precision == BGT_GPU_FP32;
+	if (request->subjects < (fp32 ? 2 : 1) || request->subjects > kServeMaxSubjects)
 	{
-		set_error("served sessions have 1 to 24 subjects");
+		set_error("served sessions have 1 to 24 subjects (2 to 24 in FP32)");
 		return BGT_GPU_UNSUPPORTED;
 	}
 	if (request->dilution != 0 && request->dilution != 1)
@@ -554,7 +561,7 @@ int bgt_gpu_server_submit(bgt_gpu_server *server, const bgt_serve_request *reque
 		return BGT_GPU_UNSUPPORTED;
 	}
 	const LatticeGeometry g = make_geometry(request->subjects, 1, true);
-	if (layout_for(g).bytes > server->cfg.memory_budget)
+	if (layout_for(g, fp32).bytes > server->cfg.memory_budget)
 	{
 		set_error("the session is larger than the server's memory budget");
 		return BGT_GPU_UNSUPPORTED;

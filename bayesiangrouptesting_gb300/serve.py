@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass
-from typing import Dict, List, Optional
+from typing import List, Optional
 
 import numpy as np
 
@@ -56,7 +56,7 @@ class SessionResult:
     neg_masks: np.ndarray
 
 
-def session_bytes(subjects: int) -> int:
+def session_bytes(subjects: int, fp32: bool = False) -> int:
     """Device bytes one served session holds (posterior + zeta partial sums
     + tables), as the server counts them against its budget."""
     # Mirrors the layout of serve.cu: each buffer rounded up to 256 bytes.
@@ -69,19 +69,18 @@ def session_bytes(subjects: int) -> int:
     w = min(w, 1 << tbits)
     nblk = (1 << tbits) // w
     states, rows = 1 << subjects, 1 << hbits
-    return (up(8 * states) * 2 + up(8 * rows) + up(4 * rows) + up(8 * nblk) + up(4 * nblk) + up(8 << tbits)
-            + up(8 * rows) + up(8 * subjects * (subjects + 1)))
+    return (up((4 if fp32 else 8) * states) + up(8 * states) + up(8 * rows) + up(4 * rows) + up(8 * nblk)
+            + up(4 * nblk) + up(8 << tbits) + up(8 * rows) + up(8 * subjects * (subjects + 1)))
 
 
 class Server:
     def __init__(self, memory_budget: int, max_sessions: int = 4096, max_stages: int = 40,
-                 threshold_up: float = 0.01, threshold_lo: float = 0.01):
+                 threshold_up: float = 0.01, threshold_lo: float = 0.01, fp32: bool = False):
         self._lib = load()
         self.max_stages = max_stages
-        cfg = ServeConfigC(memory_budget, max_sessions, max_stages, threshold_up, threshold_lo)
+        cfg = ServeConfigC(memory_budget, max_sessions, max_stages, threshold_up, threshold_lo, 1 if fp32 else 0)
         self._handle = ctypes.c_void_p()
         _call(self._lib.bgt_gpu_server_create(ctypes.byref(cfg), ctypes.byref(self._handle)))
-        self._keep: Dict[int, np.ndarray] = {}
 
     def close(self) -> None:
         h = getattr(self, "_handle", None)
@@ -149,10 +148,10 @@ class Server:
 
 
 def serve_all(requests: List[SessionRequest], memory_budget: int, max_sessions: int = 4096,
-              max_stages: int = 40, threshold_up: float = 0.01, threshold_lo: float = 0.01):
+              max_stages: int = 40, threshold_up: float = 0.01, threshold_lo: float = 0.01, fp32: bool = False):
     """Submits every request at once, drains the server and returns the
     results in request order."""
-    with Server(memory_budget, max_sessions, max_stages, threshold_up, threshold_lo) as srv:
+    with Server(memory_budget, max_sessions, max_stages, threshold_up, threshold_lo, fp32) as srv:
         tickets = [srv.submit(r) for r in requests]
         srv.run_until_idle()
         return [srv.result(t) for t in tickets]

@@ -146,6 +146,12 @@ BGT_GPU_API int bgt_gpu_lattice_read_posterior(bgt_gpu_lattice *lattice, double 
 BGT_GPU_API int bgt_gpu_lattice_posterior_probability(bgt_gpu_lattice *lattice, uint32_t state, double *out);
 BGT_GPU_API int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, double *out);
 
+/* max over states of |p_a(s) - p_b(s)| between the normalised posteriors of
+ * two lattices of the same shape, computed on the device (the FP32-vs-FP64
+ * error report; 2^30-state lattices need no host copy).  No reference
+ * counterpart: the reference compares precisions in its tests on the host. */
+BGT_GPU_API int bgt_gpu_lattice_max_abs_diff(bgt_gpu_lattice *a, bgt_gpu_lattice *b, double *out);
+
 /* Per-atom posterior masses m_i (compute_atom_masses,
  * lattice_base.cpp:25-41); `out` holds subjects*variants doubles. */
 BGT_GPU_API int bgt_gpu_lattice_atom_masses(bgt_gpu_lattice *lattice, double *out);

@@ -12,7 +12,7 @@
  * at the next round.
  *
  * No reference counterpart: the reference has no serving layer.  Sessions are
- * binary (one variant), 1 to 24 subjects, FP64; the responses come from the
+ * binary (one variant), 1 to 24 subjects (2 to 24 in FP32); the responses come from the
  * per-session streams of bgt_session_rng.h, so a served session's
  * experiments, responses and masks equal those of the same session run alone
  * (bgt_gpu_session_run_until_classified).
@@ -39,6 +39,7 @@ typedef struct bgt_serve_config
 	int max_stages;         /* stage cap per session (>= 1) */
 	double threshold_up;    /* classification thresholds (update_classification) */
 	double threshold_lo;
+	int precision;          /* BGT_GPU_FP64 or BGT_GPU_FP32 posterior storage, for every session */
 } bgt_serve_config;
 
 typedef struct bgt_serve_request
