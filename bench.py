@@ -249,7 +249,7 @@ def serve_requests(seed: int, count: int):
     return reqs, arrivals
 
 
-def run_serving(count: int):
+def run_serving(count: int, fp32: bool = False, plain: bool = True):
     """Served sessions (continuous batching) against the plain loop that runs
     the same sessions one at a time on the device.  Both are end to end:
     priors come from host memory and results land in host memory."""
@@ -260,13 +260,13 @@ def run_serving(count: int):
     reqs, arrivals = serve_requests(SERVE_SEED, count)
     # Warm-up: a small served batch and one plain session per lattice shape.
     warm, _ = serve_requests(SERVE_SEED + 1, 64)
-    with Server(8 << 30, max_sessions=64, max_stages=SERVE_STAGES) as srv:
+    with Server(8 << 30, max_sessions=64, max_stages=SERVE_STAGES, fp32=fp32) as srv:
         for r in warm:
             srv.submit(r)
         srv.run_until_idle()
     launches0 = _native.launches()
     with Server(SERVE_BUDGET, max_sessions=count, max_stages=SERVE_STAGES, threshold_up=THRESHOLD,
-                threshold_lo=THRESHOLD) as srv:
+                threshold_lo=THRESHOLD, fp32=fp32) as srv:
         tickets = [0] * count
         nxt = 0
         t0 = time.perf_counter()
@@ -290,7 +290,16 @@ def run_serving(count: int):
     round_ms = 1e3 * (done - launch)
     stage_lat = np.repeat(round_ms, sessions)
     sess_lat = np.array([r.finish_s - r.submit_s for r in served]) * 1e3
-
+    summary = {
+        "sessions_per_s": count / served_wall, "session_stages_per_s": int(stages.sum()) / served_wall,
+        "wall_s": served_wall, "rounds": int(len(launch)), "mean_sessions_per_round": float(sessions.mean()),
+        "stage_latency_ms": {"p50": float(np.percentile(stage_lat, 50)), "p99": float(np.percentile(stage_lat, 99))},
+        "session_latency_ms": {"p50": float(np.percentile(sess_lat, 50)), "p99": float(np.percentile(sess_lat, 99))},
+        "stages_per_session": float(stages.mean()), "gpu_launches": int(served_launches),
+        "algorithmic_gbs": float(sum(r.stages * 32 * (1 << r.subjects) for r in served) / served_wall / 1e9),
+    }
+    if not plain:
+        return summary, served
     # Plain loop: one session at a time through the device session loop, a
     # lattice per (n, type) reused by reset.
     lattices = {}
@@ -319,22 +328,63 @@ def run_serving(count: int):
     lattices.clear()
     total_stages = int(stages.sum())
     plain_stage_lat = plain_ms / np.maximum(stages, 1)
-    return {
+    return dict(summary, **{
         "workload": f"{count} sessions, n ~ U{{8..22}} binary, half dilution (alpha {ALPHA}, h {H}), "
                     f"pi0 ~ U[0.005, 0.15], until classified or {SERVE_STAGES} stages, Poisson arrivals "
-                    f"{SERVE_RATE:.0f}/s, {SERVE_BUDGET >> 30} GB budget, FP64",
-        "sessions_per_s": count / served_wall, "session_stages_per_s": total_stages / served_wall,
-        "wall_s": served_wall, "rounds": int(len(launch)), "mean_sessions_per_round": float(sessions.mean()),
-        "stage_latency_ms": {"p50": float(np.percentile(stage_lat, 50)), "p99": float(np.percentile(stage_lat, 99))},
-        "session_latency_ms": {"p50": float(np.percentile(sess_lat, 50)), "p99": float(np.percentile(sess_lat, 99))},
-        "stages_per_session": float(stages.mean()), "gpu_launches": int(served_launches),
+                    f"{SERVE_RATE:.0f}/s, {SERVE_BUDGET >> 30} GB budget, {'FP32' if fp32 else 'FP64'}",
         "plain_loop": {"sessions_per_s": count / plain_wall, "session_stages_per_s": total_stages / plain_wall,
                        "wall_s": plain_wall,
                        "stage_latency_ms": {"p50": float(np.percentile(plain_stage_lat, 50)),
                                             "p99": float(np.percentile(plain_stage_lat, 99))}},
         "speedup_vs_plain_loop": plain_wall / served_wall,
         "identical_to_plain_loop": bool(identical),
-    }
+    }), served
+
+
+def run_precision(stages: int = 16):
+    """Multinomial lattice n = 10 subjects x k = 3 variants (2^30 states):
+    a 16-stage Op-BBPA session in FP64 and in FP32 storage (stages/s each),
+    then the FP32 lattice replays the FP64 session's experiments and
+    responses: agreement of its own selections with the FP64 ones and the
+    max abs difference of the final normalised posteriors."""
+    import torch
+
+    import bayesiangrouptesting_gb300 as bgt
+
+    n, k = 10, 3
+    rng = np.random.default_rng(SEED + 4)
+    pi0 = rng.uniform(0.01, 0.10, n * k)
+    draws = rng.random(n * k)
+    truth = int(sum(1 << a for a in range(n * k) if draws[a] >= pi0[a]))
+    t = bgt.LatticeType.replicated_non_dilution
+    out = {"workload": f"multinomial non-dilution lattice n={n} x k={k} (2^30 states), {stages}-stage Op-BBPA "
+                       "session; likelihood 0.99/0.99 (the reference model)"}
+    lats = {}
+    for name, prec in (("fp64", bgt.Precision.float64), ("fp32", bgt.Precision.float32)):
+        lat = bgt.Lattice(t, n, pi0, variants=k, precision=prec)
+        lat.run_session(2, truth, seed=SEED, session=0)  # warm-up
+        times = []
+        for rep in range(3):
+            lat.reset(pi0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            lat.run_session(stages, truth, seed=SEED, session=1 + rep)
+            times.append(time.perf_counter() - t0)
+        out[f"{name}_stages_per_s"] = stages / statistics.median(times)
+        out[f"{name}_bytes_per_state"] = 8 if name == "fp64" else 4
+        lats[name] = lat
+    f64, f32 = lats["fp64"], lats["fp32"]
+    f64.reset(pi0)
+    f32.reset(pi0)
+    ref = f64.run_session(stages, truth, seed=SEED, session=99)
+    agree = 0
+    for e, r in zip(ref["experiments"], ref["responses"]):
+        agree += int(f32.select_experiment() == int(e))
+        f32.update(int(e), int(r))
+    out["selection_agreement"] = agree / stages
+    out["max_abs_posterior_error"] = f64.max_abs_diff(f32)
+    out["fp32_speedup"] = out["fp32_stages_per_s"] / out["fp64_stages_per_s"]
+    return out
 
 
 def run_gpu(args, world, rank, local):
@@ -430,11 +480,19 @@ def run_gpu(args, world, rank, local):
         cv, cwall = cpu_baseline(stages=args.cpu_stages, workers=1)
         cpu = {"value": cv, "unit": "stages/s", "cores": 1, "kind": "port",
                "sample": f"one n=24 session, {args.cpu_stages} stages, oracle port on 1 core ({cwall:.1f} s)"}
+    precision = None
+    if rank == 0 and world == 1 and not args.no_precision:
+        precision = run_precision()
     serving = None
     if rank == 0 and world == 1 and args.serve_sessions > 0:
         with ClockSampler(local) as serve_clocks:
-            serving = run_serving(args.serve_sessions)
+            serving, served64 = run_serving(args.serve_sessions)
+            fp32_summary, served32 = run_serving(args.serve_sessions, fp32=True, plain=False)
         serving["clocks"] = serve_clocks.summary()
+        same = sum(int(a.stages == b.stages and np.array_equal(a.experiments, b.experiments))
+                   for a, b in zip(served64, served32))
+        fp32_summary["sessions_identical_to_fp64"] = same / len(served64)
+        serving["fp32"] = fp32_summary
     line = {
         "metric": METRIC, "value": value, "unit": "stages/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
@@ -451,6 +509,7 @@ def run_gpu(args, world, rank, local):
         "clocks": clocks.summary(),
         "gpu_launches": launches,
         "serving": serving,
+        "precision": precision,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -469,6 +528,7 @@ def main():
     ap.add_argument("--cpu-stages", type=int, default=3, help="stages in the bounded CPU-baseline sample")
     ap.add_argument("--ref-stages", type=int, default=2, help="stages per core per step in the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the FP64-vs-FP32 n=10 x k=3 measurement")
     ap.add_argument("--serve-sessions", type=int, default=SERVE_SESSIONS,
                     help="sessions in the served-workload measurement (0: skip it)")
     args = ap.parse_args()
