@@ -1,6 +1,8 @@
 // Host side of the GB300 lattice provider: device-lattice handles, stage
 // orchestration (K1 / K2, see lattice_kernels.cuh) and the C ABI of
 // include/bgt_gpu.h.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -195,6 +197,39 @@ void dilution_rows(int n, double alpha, double h, double *flat)
 			flat[static_cast<size_t>(L - 1) * (n + 1) + r] = 1 - alpha * r / (kk * h + r);
 		}
 	}
+}
+
+void encode_m1_map(LatticeDev &h)
+{
+	static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+	if (!encode)
+	{
+		void *fn = nullptr;
+		cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+		cuda_check(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q),
+				   "driver entry point");
+		if (q != cudaDriverEntryPointSuccess || fn == nullptr)
+			throw CudaFailure("cuTensorMapEncodeTiled is not available");
+		encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+	}
+	// m1 = [nblk][rows][W] u64, W split as [W / Wa][Wa] so that no box edge
+	// exceeds 256; one box holds m1_boxz column blocks of one row.
+	const cuuint64_t W = static_cast<cuuint64_t>(h.colw);
+	const cuuint64_t rows = cuuint64_t{1} << h.hbits;
+	const cuuint64_t nblk = static_cast<cuuint64_t>(h.nblk);
+	const cuuint64_t wa = std::min<cuuint64_t>(W, 256), wb = W / wa;
+	const cuuint64_t dims[4] = {wa, wb, rows, nblk};
+	const cuuint64_t strides[3] = {wa * 8, W * 8, rows * W * 8};
+	const cuuint32_t boxz = static_cast<cuuint32_t>(std::min<cuuint64_t>(nblk, 256));
+	const cuuint32_t box[4] = {static_cast<cuuint32_t>(wa), static_cast<cuuint32_t>(wb), 1, boxz};
+	const cuuint32_t estr[4] = {1, 1, 1, 1};
+	const CUresult rc = encode(reinterpret_cast<CUtensorMap *>(h.m1_map), CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, h.m1, dims,
+							   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+							   CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	if (rc != CUDA_SUCCESS)
+		throw CudaFailure("cuTensorMapEncodeTiled failed for the zeta partial sums");
+	h.m1_boxz = static_cast<int>(boxz);
+	h.m1_stores = static_cast<int>(nblk / boxz);
 }
 
 LatticeGeometry make_geometry(int n, int k, bool wide)
@@ -549,6 +584,7 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			h.mode = kGenerate;
 			h.z_norm = 1.0;
 			h.active = g.n >= 32 ? 0xFFFFFFFFu : ((1u << g.n) - 1u);
+			encode_m1_map(h);
 			cuda_check(cudaMemcpyAsync(lat->dev, &h, sizeof(h), cudaMemcpyHostToDevice, lat->stream), "state upload");
 			lat->run_k1();
 			cuda_check(cudaStreamSynchronize(lat->stream), "create sync");

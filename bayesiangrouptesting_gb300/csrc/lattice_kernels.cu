@@ -147,6 +147,8 @@ struct LatCache
 {
 	int li;
 	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix, mbits, fp32;
+	int m1_boxz, m1_stores;
+	const void *m1_map;
 	unsigned int e, active;
 	const double *q_in;
 	double *q_out;
@@ -318,6 +320,8 @@ struct ItemCfg
 	double c_in, c_out;   // non-dilution update factors (contained / not)
 	float c_in32, c_out32; // the same for FP32 lattices
 	int k, n, radix;      // k >= 2: mixed-radix classes into g_ctab
+	const void *m1_map;   // tensor map of m1 for the zeta-partial-sum stores
+	int m1_boxz, m1_stores;
 };
 
 // Update factors in the lattice's storage type.
@@ -345,18 +349,7 @@ __device__ __forceinline__ T contained_factor(const ItemCfg &cfg, bool in)
 	else
 		return in ? cfg.c_in : cfg.c_out;
 }
-template <typename T>
-struct Vec2;
-template <>
-struct Vec2<double>
-{
-	typedef double2 type;
-};
-template <>
-struct Vec2<float>
-{
-	typedef float2 type;
-};
+
 
 // Mixed-radix likelihood class of state s for a multinomial update.
 __device__ __forceinline__ int multinomial_class(const ItemCfg &cfg, unsigned int s)
@@ -378,7 +371,6 @@ template <int kMode, typename T>
 __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int b, bool abort, u64 &total_out,
 										int &scale_out)
 {
-	typedef typename Vec2<T>::type V2;
 	T *const in = reinterpret_cast<T *>(tile_f64(b));
 	u64 *const work = work_tile();
 	const unsigned int tid = threadIdx.x;
@@ -388,57 +380,39 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	const size_t base = static_cast<size_t>(r) << tbits;
 	T *q_out = reinterpret_cast<T *>(cfg.q_out);
 	const double phi = cfg.phi;
-	// Phase A: pairs (x, x + 1) with x = map_a(tid, 2 i); register bits
-	// {0, 10, 11, 12}.  Reads the tile from the bulk-copied buffer (or the
-	// prior tables), applies the update, writes q'.
+	// Phase B layout (register bits 6..9; a warp reads 32 consecutive
+	// values of the bulk-copied tile, conflict-free): read the tile (or
+	// generate the prior), apply the update, write q' back for its bulk store.
 	T v[kPerThread];
 	float f = 0.0f;
 	bool bad = false;
 #pragma unroll
-	for (int i = 0; i < kPerThread / 2; i++)
+	for (int j = 0; j < kPerThread; j++)
 	{
-		const unsigned int x = map_a(tid, 2 * i);
-		V2 p;
-		p.x = T(0);
-		p.y = T(0);
+		const unsigned int x = map_b(tid, j);
+		T p = T(0);
 		if (x < tsize)
 		{
 			if (kMode == kGenerate)
-			{
-				const double2 lo = *reinterpret_cast<const double2 *>(cfg.prior_lo + x);
-				p.x = static_cast<T>(phi * lo.x);
-				p.y = static_cast<T>(phi * lo.y);
-			}
+				p = static_cast<T>(phi * cfg.prior_lo[x]);
 			else
-			{
-				p = *reinterpret_cast<const V2 *>(in + x);
-			}
+				p = in[x];
 			if (kMode == kUpdate)
 			{
 				const unsigned int s0 = static_cast<unsigned int>(base) | x;
 				if (cfg.k > 1)
-				{
-					p.x *= multinomial_factor<T>(multinomial_class(cfg, s0));
-					p.y *= multinomial_factor<T>(multinomial_class(cfg, s0 | 1u));
-				}
+					p *= multinomial_factor<T>(multinomial_class(cfg, s0));
 				else if (cfg.dilution_classes)
-				{
-					p.x *= class_factor<T>(__popc(e & s0));
-					p.y *= class_factor<T>(__popc(e & (s0 | 1u)));
-				}
+					p *= class_factor<T>(__popc(e & s0));
 				else
-				{
-					p.x *= contained_factor<T>(cfg, (e & s0) == e);
-					p.y *= contained_factor<T>(cfg, (e & (s0 | 1u)) == e);
-				}
+					p *= contained_factor<T>(cfg, (e & s0) == e);
 			}
 			if (kMode != kLoad)
-				*reinterpret_cast<V2 *>(in + x) = p; // q', bulk-stored by the caller
+				in[x] = p; // q', bulk-stored by the caller
 		}
-		v[2 * i] = p.x;
-		v[2 * i + 1] = p.y;
-		f += approx_scaled_hi(p.x) + approx_scaled_hi(p.y);
-		bad |= non_finite(p.x) | non_finite(p.y);
+		v[j] = p;
+		f += approx_scaled_hi(p);
+		bad |= non_finite(p);
 	}
 	if (bad)
 		ps.flag = 1;
@@ -460,14 +434,6 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	for (int j = 0; j < kPerThread; j++)
 		a[j] = to_fixed_fast(v[j], scale);
 	const unsigned int mask = tsize - 1u;
-	levels_a(a, mask);
-#pragma unroll
-	for (int j = 0; j < kPerThread; j++)
-		work[tile_swz(map_a(tid, j))] = a[j];
-	__syncthreads();
-#pragma unroll
-	for (int j = 0; j < kPerThread; j++)
-		a[j] = work[tile_swz(map_b(tid, j))];
 	levels_b(a, mask);
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
@@ -477,49 +443,42 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	for (int j = 0; j < kPerThread; j++)
 		a[j] = work[tile_swz(map_c(tid, j))];
 	levels_c(a, mask);
+	// Tile bit 1 is lane bit 1 in this layout: one shuffle level.
+	if (mask & 2u)
+	{
+		const bool low = (tid & 2u) == 0u;
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+		{
+			const u64 o = __shfl_xor_sync(0xFFFFFFFFu, a[j], 2);
+			a[j] += low ? o : 0ull;
+		}
+	}
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
 		work[tile_swz(map_c(tid, j))] = a[j];
 	__syncthreads();
-	// Phase D: thread t holds columns 16 t .. 16 t + 15; tile bit 1 remains.
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
-		a[j] = work[tile_swz(map_d(tid, j))];
-	reg_level(a, 1, 1, mask);
-	const unsigned int rows = 1u << cfg.hbits;
-	const int colw = cfg.colw, logw = cfg.logw;
-	const unsigned int c0 = tid << 4;
-	if (c0 < tsize)
+		a[j] = work[tile_swz(map_a(tid, j))];
+	levels_a(a, mask);
+	// The finished tile, in column order (pairs: conflict-free), is stored to
+	// m1 by the tensor map: column block c of row r lands at
+	// m1[(c * 2^hbits + r) * W].
+	__syncthreads();
+#pragma unroll
+	for (int i = 0; i < kPerThread / 2; i++)
+		*reinterpret_cast<ulonglong2 *>(work + map_a(tid, 2 * i)) = make_ulonglong2(a[2 * i], a[2 * i + 1]);
+	proxy_fence();
+	__syncthreads();
+	if (threadIdx.x == 0)
 	{
-		if (colw >= 4)
-		{
-			// Column chunks of W >= 4 values: one full 32-byte sector per store.
-#pragma unroll
-			for (int j = 0; j < kPerThread; j += 4)
-			{
-				const unsigned int col = c0 + j;
-				if (col < tsize)
-				{
-					u64 *dst = cfg.m1 + (static_cast<size_t>(col >> logw) * rows + r) * colw + (col & (colw - 1));
-					st_global_v4_u64(dst, a[j], a[j + 1], a[j + 2], a[j + 3]);
-				}
-			}
-		}
-		else
-		{
-#pragma unroll
-			for (int j = 0; j < kPerThread; j += 2)
-			{
-				const unsigned int col = c0 + j;
-				if (col < tsize)
-				{
-					u64 *dst = cfg.m1 + (static_cast<size_t>(col >> logw) * rows + r) * colw + (col & (colw - 1));
-					*reinterpret_cast<ulonglong2 *>(dst) = make_ulonglong2(a[j], a[j + 1]);
-				}
-			}
-		}
+		const int step = cfg.m1_boxz * cfg.colw;
+		for (int k = 0; k < cfg.m1_stores; k++)
+			tensor_store_4d(cfg.m1_map, work + k * step, 0, 0, static_cast<int>(r), k * cfg.m1_boxz);
+		bulk_commit();
 	}
-	total_out = a[0];
+	total_out = a[0]; // element 0 of the finished tile: the tile total
 	scale_out = scale;
 	return false;
 }
@@ -590,6 +549,9 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.dilution = L.dilution;
 			c.skip = L.skip;
 			c.fp32 = L.fp32;
+			c.m1_boxz = L.m1_boxz;
+			c.m1_stores = L.m1_stores;
+			c.m1_map = L.m1_map;
 			c.n = L.n;
 			c.k = k;
 			c.radix = radix;
@@ -638,6 +600,8 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 		load_class_table(wm_state(states, wm, l0));
 	}
 	__syncthreads();
+	if (tid == 0)
+		tensormap_acquire(ps.lc.m1_map);
 	// Thread 0 issues the bulk copy of item `item` into buffer b (no copy
 	// for generated priors or skipped lattices); same-lattice items use the
 	// cached constants.
@@ -687,20 +651,26 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 			load_lattice_cache(wm_state(states, wm, li), li);
 			load_class_table(wm_state(states, wm, li));
 			__syncthreads();
+			if (tid == 0)
+				tensormap_acquire(ps.lc.m1_map);
 		}
 		const int mode = ps.lc.mode;
 		const long long wn = w + gridDim.x;
 		const long long lat_end = w - r + items; // first item of the next lattice
-		if (tid == 0 && wn < total)
+		if (tid == 0)
 		{
 			// Buffer b ^ 1 may still be the source of the previous tile's q'
-			// bulk store.
+			// bulk store, and the work tile that of its zeta-partial-sum
+			// stores (this item writes the work tile after the next barrier).
 			bulk_wait_read_all();
-			proxy_fence();
-			if (b)
-				inflight0 = issue(wn, 0);
-			else
-				inflight1 = issue(wn, 1);
+			if (wn < total)
+			{
+				proxy_fence();
+				if (b)
+					inflight0 = issue(wn, 0);
+				else
+					inflight1 = issue(wn, 1);
+			}
 		}
 		if (ps.lc.skip)
 			continue; // a finished session: no copy was issued for it
@@ -735,6 +705,9 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 		cfg.c_out = ps.lc.c_out;
 		cfg.c_in32 = static_cast<float>(ps.lc.c_in);
 		cfg.c_out32 = static_cast<float>(ps.lc.c_out);
+		cfg.m1_map = ps.lc.m1_map;
+		cfg.m1_boxz = ps.lc.m1_boxz;
+		cfg.m1_stores = ps.lc.m1_stores;
 		cfg.k = ps.lc.k;
 		cfg.n = ps.lc.n;
 		cfg.radix = ps.lc.radix;

@@ -133,6 +133,12 @@ struct LatticeDev
 	unsigned int *out_e, *out_r, *out_pos, *out_neg;
 	int sess_stop;                 // end once every atom is classified (else run all stages)
 	SessionStatus *status;         // optional progress record
+	// ---- K1's zeta-partial-sum stores (host-encoded TMA tensor map) ----
+	// m1 viewed as the 4-D tensor [nblk][2^hbits][W / Wa][Wa] of u64
+	// (Wa = min(W, 256)); one tile row r is stored with m1_stores tensor
+	// stores of m1_boxz column blocks each, from the tile in column order.
+	int m1_boxz, m1_stores;
+	alignas(64) unsigned char m1_map[128];
 };
 
 // Work items of a batched launch.  Lattice li owns the items

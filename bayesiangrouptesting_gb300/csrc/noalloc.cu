@@ -22,6 +22,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <string>
 
 #include "bgt_gpu.h"
@@ -70,9 +71,15 @@ static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 constexpr int kMaxDevices = 64;
 NoAllocScratch *g_scratch_addr[kMaxDevices] = {};
 
+// The 128-byte tensor map of the scratch's zeta partial sums, passed by value.
+struct MapBytes
+{
+	unsigned long long w[16];
+};
+
 // Fills the pass state for a load-only selection of `posterior` (device code
 // names the scratch directly).
-__global__ void noalloc_setup(const double *posterior, LatticeGeometry g)
+__global__ void noalloc_setup(const double *posterior, LatticeGeometry g, MapBytes map, int boxz, int stores)
 {
 	if (threadIdx.x != 0 || blockIdx.x != 0)
 		return;
@@ -114,6 +121,10 @@ __global__ void noalloc_setup(const double *posterior, LatticeGeometry g)
 	L.k1_count = 0;
 	L.k2_count = 0;
 	L.sess_active = 0;
+	L.m1_boxz = boxz;
+	L.m1_stores = stores;
+	for (int i = 0; i < 16; i++)
+		reinterpret_cast<unsigned long long *>(L.m1_map)[i] = map.w[i];
 }
 
 // Writes the selection (or 0xFFFFFFFF after a device-detected error).
@@ -203,7 +214,17 @@ extern "C" int bgt_gpu_select_noalloc(const double *posterior, int subjects, int
 	{
 		const cudaStream_t s = static_cast<cudaStream_t>(stream);
 		const LatticeGeometry g = make_geometry(subjects, 1);
-		noalloc_setup<<<1, 32, 0, s>>>(posterior, g);
+		// K1 stores its zeta partial sums through a tensor map of the
+		// scratch (encoded on the host; nothing is allocated).
+		LatticeDev hm{};
+		hm.m1 = scratch->m1;
+		hm.colw = g.colw;
+		hm.hbits = g.hbits;
+		hm.nblk = g.nblk;
+		encode_m1_map(hm);
+		MapBytes mb;
+		std::memcpy(&mb, hm.m1_map, sizeof(mb));
+		noalloc_setup<<<1, 32, 0, s>>>(posterior, g, mb, hm.m1_boxz, hm.m1_stores);
 		cuda_check(cudaGetLastError(), "noalloc setup launch");
 		count_launches(1);
 		// The pass state is the scratch's first member.

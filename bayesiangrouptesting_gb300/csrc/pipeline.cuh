@@ -58,6 +58,22 @@ __device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t 
 				 : "memory");
 }
 
+// Tensor store of one 4-D box from shared memory (column order) to global
+// memory through the tensor map at `map` (global memory, 64-byte aligned).
+__device__ __forceinline__ void tensor_store_4d(const void *map, const void *src, int c0, int c1, int c2, int c3)
+{
+	asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(map),
+				 "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+				 : "memory");
+}
+
+// Orders earlier generic-proxy writes of a tensor map in global memory
+// (host copies, device kernels) before this thread's tensor operations on it.
+__device__ __forceinline__ void tensormap_acquire(const void *map)
+{
+	asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 
 // Waits until the issuing thread's committed bulk stores have finished

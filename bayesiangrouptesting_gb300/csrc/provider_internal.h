@@ -37,6 +37,10 @@ LatticeGeometry make_geometry(int n, int k, bool wide = false);
 // The dilution response table DilutionTable(n, alpha, h) flattened as
 // [(L - 1) * (n + 1) + r] (dilution.cpp:10-26).
 void dilution_rows(int n, double alpha, double h, double *flat);
+// Encodes the TMA tensor map through which K1 stores a lattice's zeta partial
+// sums (m1, colw, hbits and nblk must be set); fills m1_map, m1_boxz and
+// m1_stores.  Host-only, allocates nothing.
+void encode_m1_map(LatticeDev &state);
 int check_supported(int subjects, int variants, int dilution, std::string *why);
 void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);
 void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream);

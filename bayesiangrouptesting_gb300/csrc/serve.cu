@@ -380,6 +380,7 @@ struct bgt_gpu_server
 			h.out_neg = o + 3 * S;
 			h.sess_stop = 1;
 			h.status = status_dev + slot;
+			encode_m1_map(h);
 			a.slot = slot;
 			std::copy(rs.p.prior.begin(), rs.p.prior.end(), a.pi0);
 			a.dil_len = 0;

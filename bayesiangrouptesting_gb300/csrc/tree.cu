@@ -266,6 +266,10 @@ void bind_level_buffers(Level &lv, const LatticeGeometry &g, size_t i, LatticeDe
 	d.blk_e = lv.blk_e + (i * g.nblk << g.mbits);
 	d.m2 = lv.m2 ? lv.m2 + i * states : nullptr;
 	d.ftab = lv.ftab ? lv.ftab + i * (size_t{1} << (g.n + g.k)) : nullptr;
+	d.colw = g.colw;
+	d.hbits = g.hbits;
+	d.nblk = g.nblk;
+	encode_m1_map(d);
 }
 
 void flatten_preorder(const std::vector<HostNode> &tree, int node, std::vector<SweepNode> &out, int atoms)
