@@ -138,9 +138,17 @@ void configure_kernels()
 	done = true;
 }
 
+// The passes index work items with 32-bit arithmetic.
+void check_items(long long items)
+{
+	if (items >= (1ll << 32))
+		throw CudaFailure("a batched launch would exceed 2^32 work items");
+}
+
 void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStream_t stream)
 {
 	const long long items = static_cast<long long>(count) << g.hbits;
+	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	const WorkMap wm{count, 1 << g.hbits, nullptr, nullptr};
 	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, wm); });
@@ -154,6 +162,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	{
 		const int per_mid = g.nblk << g.mbits;
 		const long long mid_items = static_cast<long long>(count) * per_mid;
+		check_items(mid_items);
 		const int mgrid = static_cast<int>(std::min<long long>(mid_items, sm_count()));
 		const WorkMap wm_mid{count, per_mid, nullptr, nullptr};
 		timed_launch(1, stream, [&] { kmid_zeta<<<mgrid, kThreads, kPipeSmem, stream>>>(states, wm_mid); });
@@ -162,6 +171,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	}
 	const int per = g.nblk << g.mbits;
 	const long long items = static_cast<long long>(count) * per;
+	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	const WorkMap wm{count, per, nullptr, nullptr};
 	timed_launch(1, stream,
@@ -172,6 +182,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 
 void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream)
 {
+	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, wm); });
 	cuda_check(cudaGetLastError(), "k1 launch");
@@ -180,6 +191,7 @@ void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaS
 
 void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream)
 {
+	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	timed_launch(1, stream, [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(0), stream>>>(states, wm); });
 	cuda_check(cudaGetLastError(), "k2 launch");

@@ -418,6 +418,10 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 		ps.flag = 1;
 	if (kMode != kLoad)
 		proxy_fence(); // q' in shared memory -> visible to the bulk store
+	// The previous tile's zeta-partial-sum stores read the work tile, which
+	// this tile writes after the next barrier.
+	if (threadIdx.x == 0)
+		bulk_wait_read_all();
 	const float est = block_sum(f, ps.fred, abort);
 	if (abort)
 		return true;
@@ -660,9 +664,9 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 		if (tid == 0)
 		{
 			// Buffer b ^ 1 may still be the source of the previous tile's q'
-			// bulk store, and the work tile that of its zeta-partial-sum
-			// stores (this item writes the work tile after the next barrier).
-			bulk_wait_read_all();
+			// bulk store; the newest group (its zeta-partial-sum stores, from
+			// the work tile) may run on.
+			bulk_wait_read_all_but_last();
 			if (wn < total)
 			{
 				proxy_fence();

@@ -164,10 +164,12 @@ __device__ __forceinline__ int wm_find(const WorkMap &m, long long w, unsigned i
 {
 	if (m.per > 0)
 	{
-		const int li = static_cast<int>(w / m.per);
-		item = static_cast<unsigned int>(w - static_cast<long long>(li) * m.per);
+		// Launches keep their item count below 2^32: 32-bit division.
+		const unsigned int wu = static_cast<unsigned int>(w);
+		const unsigned int li = wu / static_cast<unsigned int>(m.per);
+		item = wu - li * static_cast<unsigned int>(m.per);
 		items = static_cast<unsigned int>(m.per);
-		return li;
+		return static_cast<int>(li);
 	}
 	int lo = 0, hi = m.count - 1; // the last li with prefix[li] <= w
 	while (lo < hi)

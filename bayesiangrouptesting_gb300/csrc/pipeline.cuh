@@ -80,6 +80,12 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 // reading their shared-memory source (the buffer may then be reused).
 __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 
+// The same, except for the most recent group.
+__device__ __forceinline__ void bulk_wait_read_all_but_last()
+{
+	asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+}
+
 // Waits until the issuing thread's committed bulk stores are complete.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
