@@ -99,7 +99,9 @@ void timed_launch(int pass, cudaStream_t stream, Launch &&launch)
 } // namespace
 
 void set_error(const std::string &message) { g_last_error = message; }
+bool profiling_enabled() { return g_timer.enabled; }
 void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void uncount_launches(uint64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 
 void cuda_check(cudaError_t err, const char *what)
 {

@@ -300,6 +300,28 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 		L.mode = kLoad;
 		if (tree_masses)
 			classify_atoms(L, L.up, L.lo);
+		if (L.node)
+		{
+			// Device-built tree: the node is a leaf when every atom is
+			// classified or the depth limit is reached; otherwise the
+			// candidates are the subjects with an unclassified atom (the
+			// subjects the reference's shrunk lattice still holds,
+			// shrink_plan.cpp:31-54).
+			const unsigned int clas = L.pos | L.neg;
+			const bool leaf = __popc(clas) == L.atoms || L.node_stage >= L.depth_limit;
+			unsigned int act = 0;
+			for (int j = 0; j < L.n; j++)
+				for (int v = 0; v < L.k; v++)
+					if (!(clas & (1u << (v * L.n + j))))
+						act |= 1u << j;
+			L.active = act;
+			L.skip = leaf ? 1 : 0;
+			TreeNodeRec *nd = L.node;
+			nd->pos = L.pos;
+			nd->neg = L.neg;
+			nd->leaf = leaf ? 1 : 0;
+			nd->error = L.error;
+		}
 		L.k1_count = 0;
 	}
 	__syncthreads();

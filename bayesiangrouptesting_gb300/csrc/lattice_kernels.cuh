@@ -69,6 +69,18 @@ enum K1Mode : int
 	kGenerate = 2 // q_out = prior_hi[row] * prior_lo[col]
 };
 
+// One node of a tree built on the device (complete R-ary layout: the
+// children of slot i of depth d are slots R i .. R i + R - 1 of depth d + 1).
+struct TreeNodeRec
+{
+	unsigned int ex, res;  // experiment and response on the edge from the parent
+	unsigned int pos, neg; // classification masks after the node's update
+	int stage;             // depth
+	int leaf;              // classified or at the depth limit
+	int exists;            // 0: the parent is a leaf (or missing)
+	int error;             // the lattice's error code
+};
+
 // Host-visible progress of a device-driven session (mapped pinned memory),
 // written by the selection pass after every stage.
 struct SessionStatus
@@ -138,6 +150,9 @@ struct LatticeDev
 	// (Wa = min(W, 256)); one tile row r is stored with m1_stores tensor
 	// stores of m1_boxz column blocks each, from the tile in column order.
 	int m1_boxz, m1_stores;
+	// ---- trees built on the device ----
+	TreeNodeRec *node;             // this node's record (nullptr: not a device-built tree node)
+	int node_stage, depth_limit;   // the node's depth and the search depth
 	alignas(64) unsigned char m1_map[128];
 };
 

@@ -26,7 +26,10 @@ struct LatticeGeometry
 };
 
 void set_error(const std::string &message);
+// Whether benchmark kernel timing (bgt_gpu_profile_enable) is on.
+bool profiling_enabled();
 void count_launches(uint64_t n);
+void uncount_launches(uint64_t n);
 void cuda_check(cudaError_t err, const char *what);
 void configure_kernels();
 // Tile and block shapes.  K2 blocks hold at most 16 columns by default, so

@@ -10,7 +10,10 @@
 // instead of being marginalised out; the candidate order and the zeta values
 // on the remaining subjects are those of the reference's shrunk lattice
 // (Tree::true_ex, tree.cpp:55-68, maps the compact choice back to the same
-// experiment).
+// experiment).  When the complete R-ary layout of the tree fits in device
+// memory, the tree is built entirely on the device from one CUDA graph per
+// shape (run_tree_graph); otherwise the host drives the levels and keeps only
+// the existing nodes (run_tree).  Both run the same kernels.
 //
 // Sweep: one thread per true state walks the tree in preorder, multiplying
 // branch probabilities (apply_true_state_helper, tree.cpp:174-199) and
@@ -56,6 +59,8 @@ struct SweepNode
 struct SweepParams
 {
 	int atoms, subjects, variants, dilution, count;
+	const int *count_dev; // when set, the node count lives in device memory
+	const double *thres_dev; // when set, the branch threshold lives in device memory
 	double thres;
 	const double *pi0;
 	const double *dil; // [subjects][subjects + 1]
@@ -81,6 +86,10 @@ __device__ __forceinline__ double edge_factor(const SweepParams &p, unsigned int
 __global__ void __launch_bounds__(kSweepThreads) tree_sweep(SweepParams p)
 {
 	extern __shared__ SweepNode nodes[];
+	if (p.count_dev)
+		p.count = *p.count_dev;
+	if (p.thres_dev)
+		p.thres = *p.thres_dev;
 	for (int i = threadIdx.x; i < p.count; i += blockDim.x)
 		nodes[i] = p.nodes[i];
 	__syncthreads();
@@ -174,6 +183,152 @@ __global__ void __launch_bounds__(kSweepThreads) tree_sweep(SweepParams p)
 			v += red[w][threadIdx.x];
 		p.partials[blockIdx.x * 7 + threadIdx.x] = v;
 	}
+}
+
+// ------------------------------------------------------------ device-built trees
+//
+// The whole tree of one simulation on the device, as one CUDA graph: depth d
+// holds R^d node slots (R = 2^variants; the children of slot i are slots
+// R i .. R i + R - 1 of depth d + 1), and every depth runs the same batched
+// K1 and K2 over all of its slots; slots whose parent is a leaf are skipped
+// by both passes.  K1's epilogue decides leaf / candidates per node, K2
+// selects, tree_expand fills the next depth's slots, tree_flatten writes the
+// preorder node list the sweep walks.  The launch sequence depends only on
+// the shape (subjects, variants, depth), so it is captured once and
+// replayed; the inputs (prior, dilution table, thresholds) are copied from
+// pinned host buffers by the graph itself.
+
+struct TreeFlatOut
+{
+	int count;  // preorder nodes written
+	int leaves; // leaves among them
+	int error;  // first lattice error seen, or 1 << 20 when the node capacity is exceeded
+	int pad;
+};
+
+// Fills depth d + 1 from depth d: slot c takes parent c / R's geometry and
+// tables, its own buffers from `tmpl`, and the parent's selection with
+// response c % R as its pending update (skipped unless the parent is an
+// existing internal node).
+__global__ void tree_expand(const LatticeDev *parents, LatticeDev *children, const LatticeDev *tmpl,
+							TreeNodeRec *child_nodes, int R, int nchild)
+{
+	const int c = blockIdx.x * blockDim.x + threadIdx.x;
+	if (c >= nchild)
+		return;
+	const LatticeDev &P = parents[c / R];
+	const unsigned int r = static_cast<unsigned int>(c % R);
+	const TreeNodeRec &pn = *P.node;
+	const bool exists = pn.exists && !pn.leaf;
+	LatticeDev d = P;
+	const LatticeDev &T = tmpl[c];
+	d.q_out = T.q_out;
+	d.m1 = T.m1;
+	d.m2 = T.m2;
+	d.tile_total = T.tile_total;
+	d.tile_scale = T.tile_scale;
+	d.blk_score = T.blk_score;
+	d.blk_e = T.blk_e;
+	d.ftab = T.ftab;
+	d.m1_boxz = T.m1_boxz;
+	d.m1_stores = T.m1_stores;
+	for (int i = 0; i < 128; i++)
+		d.m1_map[i] = T.m1_map[i];
+	d.node = child_nodes + c;
+	d.q_in = P.q_out;
+	d.mode = exists ? kUpdate : kLoad;
+	d.pend_e = P.best_e;
+	d.pend_r = r;
+	d.skip = exists ? 0 : 1;
+	d.error = 0;
+	d.k1_count = 0;
+	d.k2_count = 0;
+	d.node_stage = P.node_stage + 1;
+	children[c] = d;
+	TreeNodeRec nd;
+	nd.ex = P.best_e;
+	nd.res = r;
+	nd.pos = 0;
+	nd.neg = 0;
+	nd.stage = P.node_stage + 1;
+	nd.leaf = 0;
+	nd.exists = exists ? 1 : 0;
+	nd.error = 0;
+	child_nodes[c] = nd;
+}
+
+// Preorder list of the existing nodes (children in response order), with
+// each node's subtree end; one thread.
+__global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off, int depth, int R, int atoms,
+							 SweepNode *out, int capacity, TreeFlatOut *res)
+{
+	if (threadIdx.x != 0 || blockIdx.x != 0)
+		return;
+	int stack_idx[kMaxDepth + 2];
+	long long stack_slot[kMaxDepth + 2];
+	int stack_r[kMaxDepth + 2];
+	int n = 0, leaves = 0, err = 0, top = 0;
+	// Root.
+	stack_slot[0] = 0;
+	stack_r[0] = 0;
+	{
+		const TreeNodeRec &rt = recs[0];
+		SweepNode sn{};
+		sn.ex = rt.ex;
+		sn.res = rt.res;
+		sn.pos = rt.pos;
+		sn.neg = rt.neg;
+		sn.stage = 0;
+		sn.leaf = rt.leaf;
+		sn.classified = __popc(rt.pos | rt.neg) == atoms ? 1 : 0;
+		out[0] = sn;
+		stack_idx[0] = 0;
+		n = 1;
+		leaves += rt.leaf;
+		err = rt.error;
+	}
+	while (top >= 0)
+	{
+		const int d = top;
+		const long long slot = stack_slot[top];
+		const TreeNodeRec &me = recs[level_off[d] + slot];
+		if (me.leaf || d >= depth || stack_r[top] >= R)
+		{
+			out[stack_idx[top]].end = n;
+			top--;
+			continue;
+		}
+		const long long cs = slot * R + stack_r[top];
+		stack_r[top]++;
+		const TreeNodeRec &ch = recs[level_off[d + 1] + cs];
+		if (!ch.exists)
+			continue;
+		if (n >= capacity)
+		{
+			err = 1 << 20;
+			break;
+		}
+		SweepNode sn{};
+		sn.ex = ch.ex;
+		sn.res = ch.res;
+		sn.pos = ch.pos;
+		sn.neg = ch.neg;
+		sn.stage = ch.stage;
+		sn.leaf = ch.leaf;
+		sn.classified = __popc(ch.pos | ch.neg) == atoms ? 1 : 0;
+		out[n] = sn;
+		leaves += ch.leaf;
+		if (!err)
+			err = ch.error;
+		top++;
+		stack_idx[top] = n;
+		stack_slot[top] = cs;
+		stack_r[top] = 0;
+		n++;
+	}
+	res->count = n;
+	res->leaves = leaves;
+	res->error = err;
 }
 
 namespace
@@ -291,6 +446,373 @@ void flatten_preorder(const std::vector<HostNode> &tree, int node, std::vector<S
 }
 
 } // namespace
+
+// Device memory and the captured graph of one tree shape (subjects,
+// variants, depth, dilution).  Depth d uses slot set d & 1: its children
+// overwrite the states and buffers of depth d - 1, which depth d's K1 no
+// longer needs.  Only the most recent shape is kept.
+struct TreeGraph
+{
+	int subjects = 0, variants = 0, depth = 0, dilution = 0;
+	LatticeGeometry g;
+	int R = 2;
+	long long slots = 0;      // R^depth: slots per set
+	long long total_nodes = 0; // sum over depths of R^d
+	std::vector<void *> allocs;
+	LatticeDev *states[2] = {nullptr, nullptr};
+	LatticeDev *tmpl[2] = {nullptr, nullptr};
+	TreeNodeRec *recs = nullptr;
+	long long *level_off = nullptr;
+	SweepNode *flat = nullptr;
+	TreeFlatOut *flat_out = nullptr;
+	double *partials = nullptr;
+	double *d_pi0 = nullptr, *d_dil = nullptr, *d_lo = nullptr, *d_hi = nullptr, *d_thres = nullptr;
+	// Pinned inputs and outputs the graph copies from and to.
+	double *h_pi0 = nullptr, *h_dil = nullptr, *h_thres = nullptr, *h_partials = nullptr;
+	LatticeDev *h_root = nullptr;
+	TreeNodeRec *h_rootrec = nullptr;
+	TreeFlatOut *h_out = nullptr;
+	int sweep_blocks = 0;
+	cudaStream_t stream = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	uint64_t kernels_per_run = 0;
+
+	~TreeGraph()
+	{
+		if (stream)
+			cudaStreamSynchronize(stream);
+		if (exec)
+			cudaGraphExecDestroy(exec);
+		for (void *p : allocs)
+			cudaFree(p);
+		cudaFreeHost(h_pi0);
+		cudaFreeHost(h_dil);
+		cudaFreeHost(h_thres);
+		cudaFreeHost(h_partials);
+		cudaFreeHost(h_root);
+		cudaFreeHost(h_rootrec);
+		cudaFreeHost(h_out);
+		if (stream)
+			cudaStreamDestroy(stream);
+	}
+
+	template <typename T>
+	T *dev(size_t count, const char *what)
+	{
+		void *p = nullptr;
+		cuda_check(cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(T)), what);
+		allocs.push_back(p);
+		return static_cast<T *>(p);
+	}
+};
+
+std::unique_ptr<TreeGraph> g_tree_graph;
+
+// Device bytes of one slot set's buffers per slot.
+size_t tree_slot_bytes(const LatticeGeometry &g)
+{
+	const size_t states = size_t{1} << g.atoms;
+	const size_t rows = size_t{1} << g.hbits;
+	size_t b = states * 16 + rows * 12 + (static_cast<size_t>(g.nblk) << g.mbits) * 12 + sizeof(LatticeDev) * 2;
+	if (g.mbits)
+		b += states * 8;
+	if (g.k > 1)
+		b += (size_t{1} << (g.n + g.k)) * 8;
+	return b;
+}
+
+// Whether the device-built tree fits: node capacity of the sweep and a
+// device-memory budget for the two slot sets.
+bool tree_graph_fits(const LatticeGeometry &g, int variants, int depth)
+{
+	const int R = 1 << variants;
+	long long slots = 1, total = 1;
+	for (int d = 0; d < depth; d++)
+	{
+		slots *= R;
+		total += slots;
+		if (total > (1 << 16))
+			return false;
+	}
+	size_t free_b = 0, total_b = 0;
+	if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return false;
+	}
+	const double need = 2.0 * static_cast<double>(slots) * static_cast<double>(tree_slot_bytes(g));
+	return need < 0.5 * static_cast<double>(free_b) && need < 64.0e9;
+}
+
+void build_tree_graph(TreeGraph &t)
+{
+	const LatticeGeometry &g = t.g;
+	const size_t states = size_t{1} << g.atoms;
+	const size_t rows = size_t{1} << g.hbits;
+	const size_t nb = static_cast<size_t>(g.nblk) << g.mbits;
+	cuda_check(cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking), "tree stream");
+	t.R = 1 << t.variants;
+	t.slots = 1;
+	t.total_nodes = 1;
+	std::vector<long long> off(static_cast<size_t>(t.depth) + 2, 0);
+	for (int d = 0; d < t.depth; d++)
+	{
+		t.slots *= t.R;
+		off[static_cast<size_t>(d) + 1] = t.total_nodes;
+		t.total_nodes += t.slots;
+	}
+	off[static_cast<size_t>(t.depth) + 1] = t.total_nodes;
+	const size_t S = static_cast<size_t>(t.slots);
+	t.recs = t.dev<TreeNodeRec>(static_cast<size_t>(t.total_nodes), "alloc tree records");
+	t.level_off = t.dev<long long>(off.size(), "alloc level offsets");
+	cuda_check(cudaMemcpy(t.level_off, off.data(), off.size() * sizeof(long long), cudaMemcpyHostToDevice),
+			   "level offsets up");
+	t.flat = t.dev<SweepNode>(kMaxTreeNodes, "alloc sweep nodes");
+	t.flat_out = t.dev<TreeFlatOut>(1, "alloc flatten result");
+	t.d_pi0 = t.dev<double>(static_cast<size_t>(g.atoms), "alloc pi0");
+	t.d_dil = t.dev<double>(static_cast<size_t>(g.n) * (g.n + 1), "alloc dilution");
+	t.d_lo = t.dev<double>(size_t{1} << g.tbits, "alloc prior lo");
+	t.d_hi = t.dev<double>(rows, "alloc prior hi");
+	t.d_thres = t.dev<double>(1, "alloc threshold");
+	int sms = sm_count();
+	const unsigned long long total = 1ull << g.atoms;
+	t.sweep_blocks = static_cast<int>(
+		std::min<unsigned long long>(static_cast<unsigned long long>(sms) * 8, (total + kSweepThreads - 1) / kSweepThreads));
+	t.partials = t.dev<double>(static_cast<size_t>(t.sweep_blocks) * 7, "alloc partials");
+	cuda_check(cudaHostAlloc(&t.h_pi0, g.atoms * sizeof(double), cudaHostAllocDefault), "pinned pi0");
+	cuda_check(cudaHostAlloc(&t.h_dil, std::max<size_t>(1, static_cast<size_t>(g.n) * (g.n + 1)) * sizeof(double),
+							 cudaHostAllocDefault),
+			   "pinned dilution");
+	cuda_check(cudaHostAlloc(&t.h_thres, sizeof(double), cudaHostAllocDefault), "pinned threshold");
+	cuda_check(cudaHostAlloc(&t.h_partials, static_cast<size_t>(t.sweep_blocks) * 7 * sizeof(double),
+							 cudaHostAllocDefault),
+			   "pinned partials");
+	cuda_check(cudaHostAlloc(&t.h_root, sizeof(LatticeDev), cudaHostAllocDefault), "pinned root");
+	cuda_check(cudaHostAlloc(&t.h_rootrec, sizeof(TreeNodeRec), cudaHostAllocDefault), "pinned root record");
+	cuda_check(cudaHostAlloc(&t.h_out, sizeof(TreeFlatOut), cudaHostAllocDefault), "pinned flatten result");
+	// Two slot sets; their buffer bindings (and tensor maps) are fixed.
+	for (int set = 0; set < 2; set++)
+	{
+		t.states[set] = t.dev<LatticeDev>(S, "alloc tree states");
+		t.tmpl[set] = t.dev<LatticeDev>(S, "alloc tree templates");
+		double *q = t.dev<double>(S * states, "alloc tree posteriors");
+		unsigned long long *m1 = t.dev<unsigned long long>(S * states, "alloc tree zeta partials");
+		unsigned long long *m2 = g.mbits ? t.dev<unsigned long long>(S * states, "alloc middle-pass partials") : nullptr;
+		unsigned long long *tt = t.dev<unsigned long long>(S * rows, "alloc tile totals");
+		int *ts = t.dev<int>(S * rows, "alloc tile scales");
+		unsigned long long *bs = t.dev<unsigned long long>(S * nb, "alloc block scores");
+		unsigned int *be = t.dev<unsigned int>(S * nb, "alloc block winners");
+		unsigned long long *ft =
+			g.k > 1 ? t.dev<unsigned long long>(S * (size_t{1} << (g.n + g.k)), "alloc feature masses") : nullptr;
+		std::vector<LatticeDev> h(S);
+		for (size_t i = 0; i < S; i++)
+		{
+			LatticeDev &d = h[i];
+			std::memset(&d, 0, sizeof(d));
+			d.q_out = q + i * states;
+			d.m1 = m1 + i * states;
+			d.m2 = m2 ? m2 + i * states : nullptr;
+			d.tile_total = tt + i * rows;
+			d.tile_scale = ts + i * rows;
+			d.blk_score = bs + i * nb;
+			d.blk_e = be + i * nb;
+			d.ftab = ft ? ft + i * (size_t{1} << (g.n + g.k)) : nullptr;
+			d.colw = g.colw;
+			d.hbits = g.hbits;
+			d.nblk = g.nblk;
+			encode_m1_map(d);
+		}
+		cuda_check(cudaMemcpy(t.tmpl[set], h.data(), S * sizeof(LatticeDev), cudaMemcpyHostToDevice),
+				   "tree templates up");
+	}
+	// The root: slot 0 of set 0 with its template's buffers.
+	LatticeDev root{};
+	cuda_check(cudaMemcpy(&root, t.tmpl[0], sizeof(LatticeDev), cudaMemcpyDeviceToHost), "root template");
+	root.n = t.subjects;
+	root.k = t.variants;
+	root.atoms = g.atoms;
+	root.tbits = g.tbits;
+	root.hbits = g.hbits;
+	root.nblk = g.nblk;
+	root.colw = g.colw;
+	root.logw = g.logw;
+	root.mbits = g.mbits;
+	root.masses_in_k2 = 0;
+	root.dilution = t.dilution;
+	root.orig_n = t.subjects;
+	root.dil = t.d_dil;
+	root.prior_lo = t.d_lo;
+	root.prior_hi = t.d_hi;
+	root.q_in = root.q_out;
+	root.mode = kGenerate;
+	root.z_norm = 1.0;
+	root.active = t.subjects >= 32 ? 0xFFFFFFFFu : ((1u << t.subjects) - 1u);
+	root.classify_on_update = 1;
+	root.node = t.recs;
+	root.node_stage = 0;
+	root.depth_limit = t.depth;
+	*t.h_root = root; // thresholds are filled per run
+	TreeNodeRec rr{};
+	rr.exists = 1;
+	*t.h_rootrec = rr;
+	// Sweep shared memory: the node capacity.
+	cuda_check(cudaFuncSetAttribute(tree_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+									static_cast<int>(kMaxTreeNodes * sizeof(SweepNode))),
+			   "sweep smem");
+}
+
+// The launch sequence of one simulation (captured once, or run directly
+// while kernel timing is enabled).  Counts and returns its kernels.
+uint64_t enqueue_tree(TreeGraph &t)
+{
+	const LatticeGeometry &g = t.g;
+	cudaStream_t s = t.stream;
+	uint64_t kernels = 0;
+	cuda_check(cudaMemcpyAsync(t.d_pi0, t.h_pi0, g.atoms * sizeof(double), cudaMemcpyHostToDevice, s), "pi0 up");
+	if (t.dilution)
+		cuda_check(cudaMemcpyAsync(t.d_dil, t.h_dil, static_cast<size_t>(g.n) * (g.n + 1) * sizeof(double),
+								   cudaMemcpyHostToDevice, s),
+				   "dilution up");
+	cuda_check(cudaMemcpyAsync(t.d_thres, t.h_thres, sizeof(double), cudaMemcpyHostToDevice, s), "threshold up");
+	cuda_check(cudaMemcpyAsync(t.states[0], t.h_root, sizeof(LatticeDev), cudaMemcpyHostToDevice, s), "root up");
+	cuda_check(cudaMemcpyAsync(t.recs, t.h_rootrec, sizeof(TreeNodeRec), cudaMemcpyHostToDevice, s),
+			   "root record up");
+	{
+		const unsigned int rows = 1u << g.hbits;
+		const unsigned int span = std::max<unsigned int>(1u << g.tbits, rows);
+		prior_tables<<<(span + 255) / 256, 256, 0, s>>>(t.d_pi0, g.atoms, g.tbits, t.d_lo, t.d_hi);
+		cuda_check(cudaGetLastError(), "prior tables");
+		count_launches(1);
+		kernels++;
+	}
+	long long count = 1, off = 0;
+	for (int d = 0; d <= t.depth; d++)
+	{
+		LatticeDev *cur = t.states[d & 1];
+		launch_k1(cur, static_cast<int>(count), g, s);
+		kernels++;
+		if (d == t.depth)
+			break;
+		launch_k2(cur, static_cast<int>(count), g, s);
+		kernels += g.mbits ? 2 : 1;
+		const long long nchild = count * t.R;
+		tree_expand<<<static_cast<unsigned int>((nchild + 127) / 128), 128, 0, s>>>(
+			cur, t.states[(d + 1) & 1], t.tmpl[(d + 1) & 1], t.recs + off + count, t.R, static_cast<int>(nchild));
+		cuda_check(cudaGetLastError(), "tree expand");
+		count_launches(1);
+		kernels++;
+		off += count;
+		count = nchild;
+	}
+	tree_flatten<<<1, 32, 0, s>>>(t.recs, t.level_off, t.depth, t.R, g.atoms, t.flat, kMaxTreeNodes, t.flat_out);
+	cuda_check(cudaGetLastError(), "tree flatten");
+	count_launches(1);
+	kernels++;
+	SweepParams sp{};
+	sp.atoms = g.atoms;
+	sp.subjects = t.subjects;
+	sp.variants = t.variants;
+	sp.dilution = t.dilution;
+	sp.count = 0;
+	sp.count_dev = &t.flat_out->count;
+	sp.thres_dev = t.d_thres;
+	sp.thres = 0.0;
+	sp.pi0 = t.d_pi0;
+	sp.dil = t.d_dil;
+	sp.nodes = t.flat;
+	sp.partials = t.partials;
+	tree_sweep<<<t.sweep_blocks, kSweepThreads, kMaxTreeNodes * sizeof(SweepNode), s>>>(sp);
+	cuda_check(cudaGetLastError(), "sweep launch");
+	count_launches(1);
+	kernels++;
+	cuda_check(cudaMemcpyAsync(t.h_partials, t.partials, static_cast<size_t>(t.sweep_blocks) * 7 * sizeof(double),
+							   cudaMemcpyDeviceToHost, s),
+			   "partials down");
+	cuda_check(cudaMemcpyAsync(t.h_out, t.flat_out, sizeof(TreeFlatOut), cudaMemcpyDeviceToHost, s), "flatten down");
+	return kernels;
+}
+
+// The device-built tree: same results as the level loop below, one graph
+// launch per simulation.
+void run_tree_graph(int use_dilution, int subjects, int variants, const double *prior, int search_depth, double up,
+					double lo, double branch_threshold, const std::vector<double> &dil_flat, bgt_tree_stats *stats)
+{
+	TreeGraph *t = g_tree_graph.get();
+	if (!t || t->subjects != subjects || t->variants != variants || t->depth != search_depth ||
+		t->dilution != use_dilution)
+	{
+		g_tree_graph.reset();
+		std::unique_ptr<TreeGraph> fresh(new TreeGraph());
+		fresh->subjects = subjects;
+		fresh->variants = variants;
+		fresh->depth = search_depth;
+		fresh->dilution = use_dilution;
+		fresh->g = make_geometry(subjects, variants);
+		build_tree_graph(*fresh);
+		g_tree_graph = std::move(fresh);
+		t = g_tree_graph.get();
+	}
+	const LatticeGeometry &g = t->g;
+	std::memcpy(t->h_pi0, prior, g.atoms * sizeof(double));
+	if (use_dilution)
+		std::memcpy(t->h_dil, dil_flat.data(), dil_flat.size() * sizeof(double));
+	*t->h_thres = branch_threshold;
+	t->h_root->up = up;
+	t->h_root->lo = lo;
+	if (profiling_enabled())
+	{
+		// Kernel timing brackets each launch with events: run uncaptured.
+		enqueue_tree(*t);
+	}
+	else
+	{
+		if (!t->exec)
+		{
+			cudaGraph_t graph = nullptr;
+			cuda_check(cudaStreamBeginCapture(t->stream, cudaStreamCaptureModeThreadLocal), "tree capture");
+			uint64_t k = 0;
+			try
+			{
+				k = enqueue_tree(*t);
+				uncount_launches(k); // captured, not run: the replay counts them
+			}
+			catch (...)
+			{
+				cudaStreamEndCapture(t->stream, &graph);
+				if (graph)
+					cudaGraphDestroy(graph);
+				throw;
+			}
+			cuda_check(cudaStreamEndCapture(t->stream, &graph), "tree capture end");
+			const cudaError_t ie = cudaGraphInstantiate(&t->exec, graph, 0);
+			cudaGraphDestroy(graph);
+			cuda_check(ie, "tree graph instantiate");
+			t->kernels_per_run = k;
+		}
+		cuda_check(cudaGraphLaunch(t->exec, t->stream), "tree graph launch");
+		count_launches(t->kernels_per_run);
+	}
+	cuda_check(cudaStreamSynchronize(t->stream), "tree sync");
+	const TreeFlatOut out = *t->h_out;
+	if (out.error == (1 << 20))
+		throw CudaFailure("tree exceeds the sweep's node capacity");
+	if (out.error)
+		throw CudaFailure(out.error == kErrZeroMass ? "posterior normalising constant is zero"
+													: (out.error == kErrTimeout ? "a bulk copy did not complete in time"
+																				 : "non-finite posterior value"));
+	double sums[7] = {0, 0, 0, 0, 0, 0, 0};
+	for (int b = 0; b < t->sweep_blocks; b++)
+		for (int j = 0; j < 7; j++)
+			sums[j] += t->h_partials[static_cast<size_t>(b) * 7 + j];
+	stats->total_leaves = out.leaves;
+	stats->correct_probability = sums[0];
+	stats->incorrect_probability = sums[1];
+	stats->false_positive_probability = sums[2];
+	stats->false_negative_probability = sums[3];
+	stats->unclassified_probability = sums[4];
+	stats->expected_stages = sums[5];
+	stats->expected_tests = sums[6];
+}
 
 // Builds the tree and evaluates TreeStats; throws CudaFailure on error.
 // Returns a status when the request is unsupported.
@@ -498,9 +1020,11 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 	sp.nodes = static_cast<SweepNode *>(d_nodes.ptr);
 	sp.partials = static_cast<double *>(d_partials.ptr);
 	const size_t smem = flat.size() * sizeof(SweepNode);
-	if (smem > 48 * 1024)
-		cuda_check(cudaFuncSetAttribute(tree_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)),
-				   "sweep smem");
+	// The attribute stays at the node capacity (the device-built tree's
+	// captured sweep launches with all of it).
+	cuda_check(cudaFuncSetAttribute(tree_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+									static_cast<int>(kMaxTreeNodes * sizeof(SweepNode))),
+			   "sweep smem");
 	tree_sweep<<<blocks, kSweepThreads, smem, stream>>>(sp);
 	cuda_check(cudaGetLastError(), "sweep launch");
 	count_launches(1);
@@ -586,6 +1110,17 @@ int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const do
 			for (int L = 1; L <= subjects; L++)
 				for (int c = 0; c <= L; c++)
 					flat[static_cast<size_t>(L - 1) * (subjects + 1) + c] = dilution[L - 1][c];
+		}
+		configure_kernels();
+		const TreeGraph *cached = g_tree_graph.get();
+		if (cached && (cached->subjects != subjects || cached->variants != variants ||
+					   cached->depth != search_depth || cached->dilution != use_dilution))
+			g_tree_graph.reset(); // a different shape: free its memory before sizing this one
+		if (tree_graph_fits(make_geometry(subjects, variants), variants, search_depth))
+		{
+			run_tree_graph(use_dilution, subjects, variants, prior, search_depth, threshold_up, threshold_lo,
+						   branch_threshold, flat, stats);
+			return BGT_GPU_OK;
 		}
 		return run_tree(use_dilution, subjects, variants, prior, search_depth, threshold_up, threshold_lo,
 						branch_threshold, resolved, flat, stats);
