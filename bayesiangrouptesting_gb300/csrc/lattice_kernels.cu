@@ -190,6 +190,9 @@ struct PipeShared
 extern __shared__ __align__(1024) unsigned char g_smem[];
 __shared__ PipeShared ps;
 __shared__ int g_shift[1 << kMaxHighBits];
+// The matching rounding offsets 2^(shift - 1) (0 for shift 0): the rescale
+// round-half-up(v / 2^s) is (v + half) >> s.
+__shared__ u64 g_half[1 << kMaxHighBits];
 // Mixed-radix likelihood classes of a multinomial update: entry
 // sum_v c_v * radix^v holds prod_v f_v(c_v) / Z (variant order, as
 // response_prob multiplies them, src/core/model/replicated_lattice.cpp:8-28).
@@ -1000,6 +1003,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	u64 *const inbuf1 = tile_u64(1);
 	u64 *const work = work_tile();
 	int *const shift = g_shift;
+	u64 *const half = g_half;
 	const unsigned int tid = threadIdx.x;
 	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
@@ -1063,7 +1067,11 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			// output is already at the global scale.
 			const unsigned int rows_c = 1u << (Lc.hbits - Lc.mbits);
 			for (unsigned int rr = tid; rr < rows_c; rr += kThreads)
-				shift[rr] = Lc.mbits ? 0 : min(Lc.tile_scale[rr] - s_g, 63);
+			{
+				const int sh = Lc.mbits ? 0 : min(Lc.tile_scale[rr] - s_g, 63);
+				shift[rr] = sh;
+				half[rr] = sh ? (1ull << (sh - 1)) : 0ull;
+			}
 			__syncthreads();
 		}
 		const long long wn = w + gridDim.x;
@@ -1113,8 +1121,9 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			{
 				p = *reinterpret_cast<const ulonglong2 *>(in + y);
 				const int rs = shift[y >> logw];
-				p.x = shr_round(p.x, rs);
-				p.y = shr_round(p.y, rs);
+				const u64 hf = half[y >> logw];
+				p.x = (p.x + hf) >> rs; // = shr_round(p.x, rs) for p.x < 2^63
+				p.y = (p.y + hf) >> rs;
 			}
 			a[2 * i] = p.x;
 			a[2 * i + 1] = p.y;
