@@ -109,6 +109,7 @@ SIGNATURES = {
     "bgt_gpu_server_step": ([c_void_p, _ip, _ip, _ip], c_int),
     "bgt_gpu_server_result": ([c_void_p, c_uint64, POINTER(ServeResultC), _up, _up, _up, _up, c_int], c_int),
     "bgt_gpu_server_rounds": ([c_void_p, c_int, c_int, _dp, _dp, _ip, _ip], c_int),
+    "bgt_gpu_server_session_bytes": ([c_void_p, c_int, POINTER(c_uint64)], c_int),
     "bgt_gpu_lattice_reset": ([c_void_p, _dp], c_int),
     "bgt_gpu_profile_enable": ([c_int], c_int),
     "bgt_gpu_profile_read": ([POINTER(c_uint64), _dp], c_int),

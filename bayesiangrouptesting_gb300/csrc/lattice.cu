@@ -246,7 +246,7 @@ void encode_m1_map(LatticeDev &h)
 	h.m1_stores = static_cast<int>(nblk / boxz);
 }
 
-LatticeGeometry make_geometry(int n, int k, bool wide)
+LatticeGeometry make_geometry(int n, int k, int colw)
 {
 	LatticeGeometry g;
 	g.n = n;
@@ -255,11 +255,12 @@ LatticeGeometry make_geometry(int n, int k, bool wide)
 	g.tbits = g.atoms < kTileBits ? g.atoms : kTileBits;
 	g.hbits = g.atoms - g.tbits;
 	g.mbits = g.hbits > kMaxHighBits ? g.hbits - kMaxHighBits : 0;
-	int w = kTileElems >> (g.hbits - g.mbits);
+	// W: 16 columns by default (enough blocks for one lattice to fill the
+	// SMs), or the requested width, within [4, min(2^tbits, 8192 / rows)].
+	const int wmax = std::min(1 << g.tbits, kTileElems >> (g.hbits - g.mbits));
+	int w = colw > 0 ? colw : kMaxColW;
 	w = std::max(w, kMinColW);
-	if (!wide)
-		w = std::min(w, kMaxColW);
-	w = std::min(w, 1 << g.tbits);
+	w = std::min(w, wmax);
 	g.colw = w;
 	g.logw = 0;
 	while ((1 << g.logw) < w)
@@ -531,7 +532,7 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 		auto *lat = new bgt_gpu_lattice();
 		try
 		{
-			lat->g = make_geometry(subjects, variants);
+			lat->g = tuned_geometry(subjects, variants, 1);
 			lat->dilution = lattice_type;
 			lat->precision = precision;
 			const LatticeGeometry &g = lat->g;
@@ -1011,10 +1012,17 @@ int session_run_impl(bgt_gpu_lattice *lattice, int selector, int stages, double 
 		// Stage loop: K2 selects (and classifies the previous update's
 		// posterior) and queues the update, K1 applies it.
 		launch_k2(lattice->dev, 1, lattice->g, lattice->stream);
+		// A stopping session is launched in chunks of stages; between
+		// chunks the host reads whether it has ended, so a session that is
+		// classified early does not queue its remaining stages.
+		constexpr int kStageChunk = 8;
 		for (int s = 0; s < stages; s++)
 		{
 			launch_k1(lattice->dev, 1, lattice->g, lattice->stream);
 			launch_k2(lattice->dev, 1, lattice->g, lattice->stream);
+			if (stop && (s + 1) % kStageChunk == 0 && s + 1 < stages &&
+				lattice->get_field<int>(offsetof(LatticeDev, sess_active)) == 0)
+				break;
 		}
 		lattice->k1_pending = false;
 		lattice->update_pending = false;

@@ -32,11 +32,13 @@ void count_launches(uint64_t n);
 void uncount_launches(uint64_t n);
 void cuda_check(cudaError_t err, const char *what);
 void configure_kernels();
-// Tile and block shapes.  K2 blocks hold at most 16 columns by default, so
-// that one lattice spreads over many CTAs; `wide` fills each block to a full
-// tile instead (batched launches, where the parallelism comes from the number
-// of lattices).
-LatticeGeometry make_geometry(int n, int k, bool wide = false);
+// Tile and block shapes.  K2 blocks hold 16 columns by default, so that one
+// lattice spreads over many CTAs; colw > 0 requests another block width
+// (clamped to what the split allows; batched launches use full tiles).
+LatticeGeometry make_geometry(int n, int k, int colw = 0);
+// The geometry with the block width the autotuner measured fastest for
+// lattices of n * k atoms launched `batch` at a time (tune.cu).
+LatticeGeometry tuned_geometry(int n, int k, int batch);
 // The dilution response table DilutionTable(n, alpha, h) flattened as
 // [(L - 1) * (n + 1) + r] (dilution.cpp:10-26).
 void dilution_rows(int n, double alpha, double h, double *flat);

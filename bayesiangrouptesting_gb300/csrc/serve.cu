@@ -33,6 +33,7 @@ namespace
 
 constexpr int kServeMaxSubjects = 24; // tile + high passes only (no middle pass)
 constexpr int kMaxAdmitPerRound = 1024;
+constexpr int kServeBatch = 256; // batch class the block width is tuned for
 constexpr size_t kAlign = 256;
 
 size_t align_up(size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
@@ -313,7 +314,7 @@ struct bgt_gpu_server
 		while (!queue.empty() && !free_slots.empty() && count < kMaxAdmitPerRound)
 		{
 			Pending &p = queue.front();
-			const LatticeGeometry g = make_geometry(p.req.subjects, 1, true);
+			const LatticeGeometry g = tuned_geometry(p.req.subjects, 1, kServeBatch);
 			const SessionLayout lay = layout_for(g, cfg.precision == BGT_GPU_FP32);
 			size_t off = 0;
 			if (!arena.alloc(lay.bytes, &off))
@@ -561,7 +562,7 @@ int bgt_gpu_server_submit(bgt_gpu_server *server, const bgt_serve_request *reque
 		set_error("unsupported selector");
 		return BGT_GPU_UNSUPPORTED;
 	}
-	const LatticeGeometry g = make_geometry(request->subjects, 1, true);
+	const LatticeGeometry g = tuned_geometry(request->subjects, 1, kServeBatch);
 	if (layout_for(g, fp32).bytes > server->cfg.memory_budget)
 	{
 		set_error("the session is larger than the server's memory budget");
@@ -626,6 +627,25 @@ int bgt_gpu_server_result(bgt_gpu_server *server, uint64_t ticket, bgt_serve_res
 		if (dst[a] && m)
 			std::memcpy(dst[a], f.out.data() + a * n, m * sizeof(uint32_t));
 	return BGT_GPU_OK;
+}
+
+int bgt_gpu_server_session_bytes(bgt_gpu_server *server, int subjects, uint64_t *bytes)
+{
+	if (!server || !bytes)
+	{
+		set_error("null server or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (subjects < 1 || subjects > kServeMaxSubjects)
+	{
+		set_error("served sessions have 1 to 24 subjects");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return server_guarded([&]() -> int {
+		const LatticeGeometry g = tuned_geometry(subjects, 1, kServeBatch);
+		*bytes = layout_for(g, server->cfg.precision == BGT_GPU_FP32).bytes;
+		return BGT_GPU_OK;
+	});
 }
 
 int bgt_gpu_server_rounds(bgt_gpu_server *server, int first, int count, double *launch_s, double *done_s,

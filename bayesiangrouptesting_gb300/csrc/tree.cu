@@ -747,7 +747,7 @@ void run_tree_graph(int use_dilution, int subjects, int variants, const double *
 		fresh->variants = variants;
 		fresh->depth = search_depth;
 		fresh->dilution = use_dilution;
-		fresh->g = make_geometry(subjects, variants);
+		fresh->g = tuned_geometry(subjects, variants, static_cast<int>(std::min<long long>(1 << 20, 1ll << (variants * search_depth))));
 		build_tree_graph(*fresh);
 		g_tree_graph = std::move(fresh);
 		t = g_tree_graph.get();
@@ -819,7 +819,7 @@ void run_tree_graph(int use_dilution, int subjects, int variants, const double *
 int run_tree(int use_dilution, int subjects, int variants, const double *prior, int search_depth, double up, double lo,
 			 double branch_threshold, int selector, const std::vector<double> &dil_flat, bgt_tree_stats *stats)
 {
-	const LatticeGeometry g = make_geometry(subjects, variants);
+	const LatticeGeometry g = tuned_geometry(subjects, variants, 16);
 	configure_kernels();
 	cudaStream_t stream = nullptr;
 	cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "tree stream");

@@ -1,0 +1,210 @@
+// Autotuner of the zeta pass split: the K2 column-block width W per lattice
+// size and batch size.
+//
+// K1 transforms the low 13 index bits of each tile in shared memory; K2
+// transforms the high bits of a block of W columns x 2^h rows.  W sets how
+// the high pass is cut into work items: narrow blocks give a single lattice
+// enough items to fill the SMs, full-tile blocks (rows x W = 8192) give
+// batched launches fewer, larger items.  Which is faster depends on the
+// lattice size and on how many lattices share a launch, so the first request
+// for a (atoms, batch class) pair times every valid W on scratch lattices
+// (K1 + K2 of a generated prior, CUDA events, best of three) and caches the
+// winner for the process.  W never changes results: the zeta sums are exact
+// integers whatever the blocking.  BGT_GB300_TUNE=0 skips the timing and
+// uses the heuristic (narrow for one lattice, full tiles for batches).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "lattice_kernels.cuh"
+#include "provider_internal.h"
+
+namespace bgt_gpu
+{
+
+__global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
+
+namespace
+{
+
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, int> g_tuned; // (atoms, batch class) -> W
+
+int batch_class(int batch) { return batch <= 1 ? 1 : (batch <= 16 ? 16 : 256); }
+
+bool tuning_enabled()
+{
+	const char *v = std::getenv("BGT_GB300_TUNE");
+	return !(v && v[0] == '0');
+}
+
+// Valid block widths for a geometry's tile / high-bit split.
+std::vector<int> width_candidates(const LatticeGeometry &base)
+{
+	std::vector<int> out;
+	const int h2 = base.hbits - base.mbits;
+	const int wmax = std::min(1 << base.tbits, kTileElems >> h2);
+	for (int w = std::min(kMinColW, 1 << base.tbits); w <= wmax; w <<= 1)
+		out.push_back(w);
+	return out;
+}
+
+struct Scratch
+{
+	std::vector<void *> ptrs;
+	~Scratch()
+	{
+		for (void *p : ptrs)
+			cudaFree(p);
+	}
+	template <typename T>
+	T *get(size_t n)
+	{
+		void *p = nullptr;
+		cuda_check(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)), "tuner scratch");
+		ptrs.push_back(p);
+		return static_cast<T *>(p);
+	}
+};
+
+// Milliseconds of one K1 (zeta of a loaded posterior) + K2 over `count`
+// lattices of geometry g; best of three.
+float time_width(const LatticeGeometry &g, int count)
+{
+	const size_t states = size_t{1} << g.atoms;
+	const size_t rows = size_t{1} << g.hbits;
+	const size_t blocks = static_cast<size_t>(g.nblk) << g.mbits;
+	configure_kernels();
+	Scratch s;
+	double *pi0 = s.get<double>(static_cast<size_t>(g.atoms));
+	double *lo = s.get<double>(size_t{1} << g.tbits);
+	double *hi = s.get<double>(rows);
+	double *q = s.get<double>(states * count);
+	unsigned long long *m1 = s.get<unsigned long long>(states * count);
+	unsigned long long *m2 = g.mbits ? s.get<unsigned long long>(states * count) : nullptr;
+	unsigned long long *tt = s.get<unsigned long long>(rows * count);
+	int *ts = s.get<int>(rows * count);
+	unsigned long long *bs = s.get<unsigned long long>(blocks * count);
+	unsigned int *be = s.get<unsigned int>(blocks * count);
+	LatticeDev *dev = s.get<LatticeDev>(static_cast<size_t>(count));
+	std::vector<double> prior(static_cast<size_t>(g.atoms), 0.05);
+	cuda_check(cudaMemcpy(pi0, prior.data(), prior.size() * sizeof(double), cudaMemcpyHostToDevice), "tuner prior");
+	cudaStream_t stream = nullptr;
+	cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "tuner stream");
+	struct StreamGuard
+	{
+		cudaStream_t s;
+		~StreamGuard() { cudaStreamDestroy(s); }
+	} guard{stream};
+	const unsigned int span = std::max<unsigned int>(1u << g.tbits, static_cast<unsigned int>(rows));
+	prior_tables<<<(span + 255) / 256, 256, 0, stream>>>(pi0, g.atoms, g.tbits, lo, hi);
+	cuda_check(cudaGetLastError(), "tuner prior tables");
+	count_launches(1);
+	std::vector<LatticeDev> h(static_cast<size_t>(count));
+	for (int i = 0; i < count; i++)
+	{
+		LatticeDev &d = h[static_cast<size_t>(i)];
+		std::memset(&d, 0, sizeof(d));
+		d.n = g.atoms;
+		d.k = 1;
+		d.atoms = g.atoms;
+		d.tbits = g.tbits;
+		d.hbits = g.hbits;
+		d.nblk = g.nblk;
+		d.colw = g.colw;
+		d.logw = g.logw;
+		d.mbits = g.mbits;
+		d.orig_n = g.atoms;
+		d.q_in = q + i * states;
+		d.q_out = q + i * states;
+		d.m1 = m1 + i * states;
+		d.m2 = m2 ? m2 + i * states : nullptr;
+		d.tile_total = tt + i * rows;
+		d.tile_scale = ts + i * rows;
+		d.blk_score = bs + i * blocks;
+		d.blk_e = be + i * blocks;
+		d.prior_lo = lo;
+		d.prior_hi = hi;
+		d.mode = kGenerate;
+		d.z_norm = 1.0;
+		d.active = g.atoms >= 32 ? 0xFFFFFFFFu : ((1u << g.atoms) - 1u);
+		encode_m1_map(d);
+	}
+	cuda_check(cudaMemcpyAsync(dev, h.data(), h.size() * sizeof(LatticeDev), cudaMemcpyHostToDevice, stream),
+			   "tuner states");
+	cudaEvent_t a = nullptr, b = nullptr;
+	cuda_check(cudaEventCreate(&a), "tuner event");
+	cuda_check(cudaEventCreate(&b), "tuner event");
+	float best = 1e30f;
+	try
+	{
+		launch_k1(dev, count, g, stream); // generate the prior (then the lattices stay in load mode)
+		launch_k2(dev, count, g, stream);
+		for (int rep = 0; rep < 3; rep++)
+		{
+			cuda_check(cudaEventRecord(a, stream), "tuner record");
+			launch_k1(dev, count, g, stream);
+			launch_k2(dev, count, g, stream);
+			cuda_check(cudaEventRecord(b, stream), "tuner record");
+			cuda_check(cudaEventSynchronize(b), "tuner sync");
+			float ms = 0.0f;
+			cuda_check(cudaEventElapsedTime(&ms, a, b), "tuner elapsed");
+			best = std::min(best, ms);
+		}
+	}
+	catch (...)
+	{
+		cudaEventDestroy(a);
+		cudaEventDestroy(b);
+		throw;
+	}
+	cudaEventDestroy(a);
+	cudaEventDestroy(b);
+	return best;
+}
+
+} // namespace
+
+LatticeGeometry tuned_geometry(int n, int k, int batch)
+{
+	const LatticeGeometry narrow = make_geometry(n, k, 0);
+	const int cls = batch_class(batch);
+	const std::vector<int> widths = width_candidates(narrow);
+	const int heuristic = cls == 1 ? narrow.colw : widths.back();
+	if (widths.size() <= 1 || !tuning_enabled())
+		return make_geometry(n, k, heuristic);
+	std::lock_guard<std::mutex> lock(g_tune_mutex);
+	const std::pair<int, int> key(narrow.atoms, cls);
+	auto it = g_tuned.find(key);
+	if (it == g_tuned.end())
+	{
+		// Scratch lattices: the batch class, at most 2 GB of posterior +
+		// partial sums.
+		const size_t per = (size_t{16} << narrow.atoms) + (size_t{1} << 16);
+		const int count = static_cast<int>(std::max<size_t>(1, std::min<size_t>(cls, (size_t{2} << 30) / per)));
+		int best_w = heuristic;
+		float best_ms = 1e30f;
+		for (int w : widths)
+		{
+			// Timed on binary lattices of the same atom count (the passes'
+			// blocking does not depend on how atoms group into variants).
+			const LatticeGeometry g = make_geometry(narrow.atoms, 1, w);
+			const float ms = time_width(g, count);
+			if (ms < best_ms)
+			{
+				best_ms = ms;
+				best_w = w;
+			}
+		}
+		it = g_tuned.emplace(key, best_w).first;
+	}
+	return make_geometry(n, k, it->second);
+}
+
+} // namespace bgt_gpu

@@ -56,23 +56,6 @@ class SessionResult:
     neg_masks: np.ndarray
 
 
-def session_bytes(subjects: int, fp32: bool = False) -> int:
-    """Device bytes one served session holds (posterior + zeta partial sums
-    + tables), as the server counts them against its budget."""
-    # Mirrors the layout of serve.cu: each buffer rounded up to 256 bytes.
-    def up(b):
-        return (b + 255) // 256 * 256
-
-    tbits = min(subjects, 13)
-    hbits = subjects - tbits
-    w = max(4, 8192 >> hbits)
-    w = min(w, 1 << tbits)
-    nblk = (1 << tbits) // w
-    states, rows = 1 << subjects, 1 << hbits
-    return (up((4 if fp32 else 8) * states) + up(8 * states) + up(8 * rows) + up(4 * rows) + up(8 * nblk)
-            + up(4 * nblk) + up(8 << tbits) + up(8 * rows) + up(8 * subjects * (subjects + 1)))
-
-
 class Server:
     def __init__(self, memory_budget: int, max_sessions: int = 4096, max_stages: int = 40,
                  threshold_up: float = 0.01, threshold_lo: float = 0.01, fp32: bool = False):
@@ -96,6 +79,13 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+    def session_bytes(self, subjects: int) -> int:
+        """Device bytes a session of `subjects` subjects holds against the
+        budget (posterior, zeta partial sums, tables)."""
+        out = ctypes.c_uint64()
+        _call(self._lib.bgt_gpu_server_session_bytes(self._handle, subjects, ctypes.byref(out)))
+        return int(out.value)
 
     def submit(self, req: SessionRequest) -> int:
         prior = np.ascontiguousarray(req.prior, dtype=np.float64)

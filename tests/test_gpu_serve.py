@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import bayesiangrouptesting_gb300 as bgt
-from bayesiangrouptesting_gb300.serve import Server, SessionRequest, serve_all, session_bytes
+from bayesiangrouptesting_gb300.serve import Server, SessionRequest, serve_all
 
 pytestmark = pytest.mark.gpu
 
@@ -83,7 +83,9 @@ def test_served_sessions_match_oracle(gpu, oracle):
 def test_admission_under_memory_and_slot_limits(gpu):
     reqs = _requests(10, seed=5, n_lo=12, n_hi=12)
     free = serve_all(reqs, memory_budget=GB)
-    budget = 3 * session_bytes(12) + 4096
+    with Server(GB, max_sessions=1) as probe:
+        one = probe.session_bytes(12)
+    budget = 3 * one + 4096
     with Server(budget, max_sessions=8) as srv:
         tickets = [srv.submit(r) for r in reqs]
         active, queued, _ = srv.step()
