@@ -996,6 +996,14 @@ __device__ void k2_epilogue(LatticeDev &L, unsigned int per)
 	__syncthreads();
 }
 
+// |2 M - Z| for 0 <= M <= Z < 2^62: the difference fits a signed 64-bit
+// word, so one three-input add and an absolute value.
+__device__ __forceinline__ u64 abs_score(u64 m, u64 zg)
+{
+	const long long d = static_cast<long long>(m + m - zg);
+	return static_cast<u64>(d < 0 ? -d : d);
+}
+
 // K2: one W-column block of M1 (all 2^h rows, contiguous) per work item.
 __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *states, WorkMap wm)
 {
@@ -1198,8 +1206,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 #pragma unroll
 			for (int j = 0; j < kPerThread; j++)
 			{
-				const u64 m2 = a[j] << 1;
-				const u64 score = m2 > zg ? m2 - zg : zg - m2;
+				const u64 score = abs_score(a[j], zg);
 				const bool take = (y0 + (j << 2)) < elems && score < best;
 				best = take ? score : best;
 				best_j = take ? j : best_j;
@@ -1212,8 +1219,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			{
 				const unsigned int y = y0 + (j << 2);
 				const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
-				const u64 m2 = a[j] << 1;
-				const u64 score = m2 > zg ? m2 - zg : zg - m2;
+				const u64 score = abs_score(a[j], zg);
 				const bool take = y < elems && (E & ~active) == 0 && score < best;
 				best = take ? score : best;
 				best_j = take ? j : best_j;

@@ -343,6 +343,36 @@ def run_serving(count: int, fp32: bool = False, plain: bool = True):
     }), served
 
 
+def run_tree(reps: int = 5):
+    """Batched tree simulation: binary non-dilution lattice n=20
+    (pi0 ~ U[0.01, 0.15]), Op-BHA to search depth 8, TreeStats over all 2^20
+    true states, through run_simulation (one graph replay per tree), against
+    the oracle port of the reference CPU provider on one host core."""
+    import bayesiangrouptesting_gb300 as bgt
+    from oracle.oracle import Oracle
+
+    n, depth = 20, 8
+    rng = np.random.default_rng(SEED + 3)
+    pi0 = rng.uniform(0.01, 0.15, n)
+    cfg = bgt.SimulationConfig(subjects=n, prior=list(pi0),
+                               options=bgt.SimulationOptions(search_depth=depth, provider=bgt.Provider.cuda))
+    bgt.run_simulation(cfg)  # builds and captures the graph, tunes the block width
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        got = bgt.run_simulation(cfg).stats.as_array()
+        times.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    want = Oracle().run_simulation(0, n, 1, pi0, depth)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"binary non-dilution n={n}, Op-BHA, search depth {depth}, TreeStats over 2^{n} true "
+                        "states (device-built tree, one CUDA graph replay)",
+            "ms_per_tree": 1e3 * statistics.median(times), "leaves": int(got[0]),
+            "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port", "sample": "the same tree, once"},
+            "speedup_vs_cpu": cpu_s / statistics.median(times),
+            "max_abs_stats_diff_vs_oracle": float(np.max(np.abs(got - want)))}
+
+
 def run_precision(stages: int = 16):
     """Multinomial lattice n = 10 subjects x k = 3 variants (2^30 states):
     a 16-stage Op-BBPA session in FP64 and in FP32 storage (stages/s each),
@@ -485,6 +515,9 @@ def run_gpu(args, world, rank, local):
     precision = None
     if rank == 0 and world == 1 and not args.no_precision:
         precision = run_precision()
+    tree = None
+    if rank == 0 and world == 1 and not args.no_tree:
+        tree = run_tree()
     serving = None
     if rank == 0 and world == 1 and args.serve_sessions > 0:
         with ClockSampler(local) as serve_clocks:
@@ -512,6 +545,7 @@ def run_gpu(args, world, rank, local):
         "gpu_launches": launches,
         "serving": serving,
         "precision": precision,
+        "tree": tree,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -524,13 +558,14 @@ def run_gpu(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-stages", type=int, default=3, help="stages in the bounded CPU-baseline sample")
     ap.add_argument("--ref-stages", type=int, default=2, help="stages per core per step in the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP64-vs-FP32 n=10 x k=3 measurement")
+    ap.add_argument("--no-tree", action="store_true", help="skip the n=20 depth-8 tree measurement")
     ap.add_argument("--serve-sessions", type=int, default=SERVE_SESSIONS,
                     help="sessions in the served-workload measurement (0: skip it)")
     args = ap.parse_args()
