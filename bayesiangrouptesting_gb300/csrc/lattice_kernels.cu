@@ -60,6 +60,34 @@ __device__ __forceinline__ unsigned int map_c(unsigned int t, int j)
 }
 __device__ __forceinline__ unsigned int map_d(unsigned int t, int j) { return static_cast<unsigned int>(j) | (t << 4); }
 
+// The swizzled index tile_swz(map_X(t, j)) in closed form: a per-thread base
+// combined with a per-j constant (an XOR on the low four bits and an offset
+// that folds into the shared-memory instruction), checked against the
+// definitions for every (t, j).
+__device__ __forceinline__ unsigned int swz_a_base(unsigned int t) { return (t << 1) ^ ((t >> 3) & 15u); }
+__device__ __forceinline__ unsigned int swz_a(unsigned int base, int j)
+{
+	return (base ^ static_cast<unsigned int>(j & 1)) + (static_cast<unsigned int>(j >> 1) << 10);
+}
+__device__ __forceinline__ unsigned int swz_b_base(unsigned int t)
+{
+	return ((t & 15u) ^ ((t >> 4) & 3u)) | (t & 48u) | ((t >> 6) << 10);
+}
+__device__ __forceinline__ unsigned int swz_b(unsigned int base, int j)
+{
+	return (base ^ (static_cast<unsigned int>(j & 3) << 2)) + (static_cast<unsigned int>(j) << 6);
+}
+__device__ __forceinline__ unsigned int swz_c_base(unsigned int t)
+{
+	return (t & 3u) | (((t >> 2) & 3u) << 2) | ((t >> 2) << 6);
+}
+__device__ __forceinline__ unsigned int swz_c(unsigned int base, int j)
+{
+	return (base ^ static_cast<unsigned int>((j >> 2) | ((j & 3) << 2))) + (static_cast<unsigned int>(j >> 2) << 4);
+}
+__device__ __forceinline__ unsigned int swz_d_base(unsigned int t) { return (t << 4) ^ (t & 15u); }
+__device__ __forceinline__ unsigned int swz_d(unsigned int base, int j) { return base ^ static_cast<unsigned int>(j); }
+
 // Zeta butterfly over register bit `lvl` when tile bit `bit` is in `mask`.
 __device__ __forceinline__ void reg_level(u64 (&a)[kPerThread], int lvl, int bit, unsigned int mask)
 {
@@ -399,6 +427,11 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	T *const in = reinterpret_cast<T *>(tile_f64(b));
 	u64 *const work = work_tile();
 	const unsigned int tid = threadIdx.x;
+	const unsigned int sa = swz_a_base(tid), sb = swz_b_base(tid), sc = swz_c_base(tid), sd = swz_d_base(tid);
+	(void)sa;
+	(void)sb;
+	(void)sc;
+	(void)sd;
 	const int tbits = cfg.tbits;
 	const unsigned int tsize = 1u << tbits;
 	const unsigned int e = cfg.e;
@@ -466,11 +499,11 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	levels_b(a, mask);
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
-		work[tile_swz(map_b(tid, j))] = a[j];
+		work[swz_b(sb, j)] = a[j];
 	__syncthreads();
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
-		a[j] = work[tile_swz(map_c(tid, j))];
+		a[j] = work[swz_c(sc, j)];
 	levels_c(a, mask);
 	// Tile bit 1 is lane bit 1 in this layout: one shuffle level.
 	if (mask & 2u)
@@ -485,11 +518,11 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	}
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
-		work[tile_swz(map_c(tid, j))] = a[j];
+		work[swz_c(sc, j)] = a[j];
 	__syncthreads();
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
-		a[j] = work[tile_swz(map_a(tid, j))];
+		a[j] = work[swz_a(sa, j)];
 	levels_a(a, mask);
 	// The finished tile, in column order (pairs: conflict-free), is stored to
 	// m1 by the tensor map: column block c of row r lands at
@@ -1013,6 +1046,11 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	int *const shift = g_shift;
 	u64 *const half = g_half;
 	const unsigned int tid = threadIdx.x;
+	const unsigned int sa = swz_a_base(tid), sb = swz_b_base(tid), sc = swz_c_base(tid), sd = swz_d_base(tid);
+	(void)sa;
+	(void)sb;
+	(void)sc;
+	(void)sd;
 	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
@@ -1139,7 +1177,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		levels_a(a, mask);
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			work[tile_swz(map_a(tid, j))] = a[j];
+			work[swz_a(sa, j)] = a[j];
 		if (__syncthreads_or(timed_out))
 		{
 			if (tid == 0)
@@ -1152,15 +1190,15 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		}
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[tile_swz(map_b(tid, j))];
+			a[j] = work[swz_b(sb, j)];
 		levels_b(a, mask);
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			work[tile_swz(map_b(tid, j))] = a[j];
+			work[swz_b(sb, j)] = a[j];
 		__syncthreads();
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[tile_swz(map_c(tid, j))];
+			a[j] = work[swz_c(sc, j)];
 		levels_c(a, mask);
 		// All row bits are done (W >= 4, so y bits 0..1 are column bits).
 		// Score |2 M(E) - Z_g|; within a thread E grows with j, so a strict
@@ -1285,6 +1323,11 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 	u64 *const inbuf1 = tile_u64(1);
 	u64 *const work = work_tile();
 	const unsigned int tid = threadIdx.x;
+	const unsigned int sa = swz_a_base(tid), sb = swz_b_base(tid), sc = swz_c_base(tid), sd = swz_d_base(tid);
+	(void)sa;
+	(void)sb;
+	(void)sc;
+	(void)sd;
 	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
@@ -1363,7 +1406,7 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 		levels_a(a, mask);
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			work[tile_swz(map_a(tid, j))] = a[j];
+			work[swz_a(sa, j)] = a[j];
 		if (__syncthreads_or(timed_out))
 		{
 			if (tid == 0)
@@ -1376,25 +1419,25 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 		}
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[tile_swz(map_b(tid, j))];
+			a[j] = work[swz_b(sb, j)];
 		levels_b(a, mask);
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			work[tile_swz(map_b(tid, j))] = a[j];
+			work[swz_b(sb, j)] = a[j];
 		__syncthreads();
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[tile_swz(map_c(tid, j))];
+			a[j] = work[swz_c(sc, j)];
 		levels_c(a, mask);
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			work[tile_swz(map_c(tid, j))] = a[j];
+			work[swz_c(sc, j)] = a[j];
 		__syncthreads();
 		// Thread t now takes block indices 16 t .. 16 t + 15: four rows of
 		// four columns, each row one 32-byte sector of the transposed output.
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[tile_swz(map_d(tid, j))];
+			a[j] = work[swz_d(sd, j)];
 #pragma unroll
 		for (int q = 0; q < 4; q++)
 		{
