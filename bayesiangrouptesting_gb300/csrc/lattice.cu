@@ -162,7 +162,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 {
 	if (g.mbits > 0)
 	{
-		const int per_mid = g.nblk << g.mbits;
+		const int per_mid = g.mid_items;
 		const long long mid_items = static_cast<long long>(count) * per_mid;
 		check_items(mid_items);
 		const int mgrid = static_cast<int>(std::min<long long>(mid_items, sm_count()));
@@ -171,7 +171,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 		cuda_check(cudaGetLastError(), "middle pass launch");
 		count_launches(1);
 	}
-	const int per = g.nblk << g.mbits;
+	const int per = g.k2_items;
 	const long long items = static_cast<long long>(count) * per;
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
@@ -266,7 +266,57 @@ LatticeGeometry make_geometry(int n, int k, int colw)
 	while ((1 << g.logw) < w)
 		g.logw++;
 	g.nblk = (1 << g.tbits) / w;
+	g.k2_items = g.nblk << g.mbits;
+	g.mid_items = g.nblk << g.mbits;
+	if (k > 1)
+	{
+		std::vector<unsigned int> blocks, cblks;
+		bbpa_block_lists(g, blocks, cblks);
+		g.k2_items = static_cast<int>(blocks.size());
+		g.mid_items = static_cast<int>(cblks.size()) << g.mbits;
+	}
 	return g;
+}
+
+void bbpa_block_lists(const LatticeGeometry &g, std::vector<unsigned int> &blocks, std::vector<unsigned int> &cblks)
+{
+	std::vector<char> hit(static_cast<size_t>(g.nblk) << g.mbits, 0), chit(static_cast<size_t>(g.nblk), 0);
+	const unsigned int tmask = (1u << g.tbits) - 1u, mmask = (1u << g.mbits) - 1u;
+	for (unsigned int B = 1; B < (1u << g.k); B++)
+		for (unsigned int E = 0; E < (1u << g.n); E++)
+		{
+			unsigned int P = 0;
+			for (int v = 0; v < g.k; v++)
+				if (B & (1u << v))
+					P |= E << (v * g.n);
+			const unsigned int cblk = (P & tmask) >> g.logw;
+			const unsigned int r_lo = (P >> g.tbits) & mmask;
+			hit[(static_cast<size_t>(cblk) << g.mbits) | r_lo] = 1;
+			chit[cblk] = 1;
+		}
+	blocks.clear();
+	cblks.clear();
+	for (size_t i = 0; i < hit.size(); i++)
+		if (hit[i])
+			blocks.push_back(static_cast<unsigned int>(i));
+	for (size_t i = 0; i < chit.size(); i++)
+		if (chit[i])
+			cblks.push_back(static_cast<unsigned int>(i));
+}
+
+void upload_block_lists(const LatticeGeometry &g, unsigned int **blocks, unsigned int **cblks)
+{
+	*blocks = nullptr;
+	*cblks = nullptr;
+	if (g.k < 2)
+		return;
+	std::vector<unsigned int> b, c;
+	bbpa_block_lists(g, b, c);
+	cuda_check(cudaMalloc(blocks, b.size() * sizeof(unsigned int)), "alloc block list");
+	cuda_check(cudaMalloc(cblks, c.size() * sizeof(unsigned int)), "alloc column-block list");
+	cuda_check(cudaMemcpy(*blocks, b.data(), b.size() * sizeof(unsigned int), cudaMemcpyHostToDevice), "block list up");
+	cuda_check(cudaMemcpy(*cblks, c.data(), c.size() * sizeof(unsigned int), cudaMemcpyHostToDevice),
+			   "column-block list up");
 }
 
 // Validates a request against what this build supports; returns 0 or a status.
@@ -326,6 +376,7 @@ struct bgt_gpu_lattice
 	double *q = nullptr;
 	unsigned long long *m1 = nullptr;
 	unsigned long long *m2 = nullptr;
+	unsigned int *blk_list = nullptr, *cblk_list = nullptr; // k >= 2: blocks BBPA reads
 	unsigned long long *tile_total = nullptr;
 	int *tile_scale = nullptr;
 	unsigned long long *blk_score = nullptr;
@@ -349,6 +400,8 @@ struct bgt_gpu_lattice
 		cudaFree(q);
 		cudaFree(m1);
 		cudaFree(m2);
+		cudaFree(blk_list);
+		cudaFree(cblk_list);
 		cudaFree(tile_total);
 		cudaFree(tile_scale);
 		cudaFree(blk_score);
@@ -583,6 +636,9 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			h.m2 = lat->m2;
 			h.masses_in_k2 = 1;
 			h.fp32 = precision == BGT_GPU_FP32 ? 1 : 0;
+			upload_block_lists(g, &lat->blk_list, &lat->cblk_list);
+			h.blk_list = lat->blk_list;
+			h.cblk_list = lat->cblk_list;
 			h.dilution = lattice_type;
 			h.orig_n = subjects;
 			h.q_in = lat->q;

@@ -177,6 +177,7 @@ struct LatCache
 	int mode, tbits, hbits, colw, logw, dilution, skip, n, k, radix, mbits, fp32;
 	int m1_boxz, m1_stores;
 	const void *m1_map;
+	const unsigned int *blk_list, *cblk_list;
 	unsigned int e, active;
 	const double *q_in;
 	double *q_out;
@@ -614,6 +615,8 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.m1_boxz = L.m1_boxz;
 			c.m1_stores = L.m1_stores;
 			c.m1_map = L.m1_map;
+			c.blk_list = L.blk_list;
+			c.cblk_list = L.cblk_list;
 			c.n = L.n;
 			c.k = k;
 			c.radix = radix;
@@ -1068,6 +1071,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		const int li = wm_find(wm, item, blk, bcount);
 		int skip, hbits, colw, mbits;
 		u64 *src;
+		const unsigned int *list;
 		if (li == ps.lc.li)
 		{
 			skip = ps.lc.skip;
@@ -1075,6 +1079,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			colw = ps.lc.colw;
 			mbits = ps.lc.mbits;
 			src = mbits ? ps.lc.m2 : ps.lc.m1;
+			list = ps.lc.blk_list;
 		}
 		else
 		{
@@ -1084,9 +1089,12 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			colw = Ln.colw;
 			mbits = Ln.mbits;
 			src = mbits ? Ln.m2 : Ln.m1;
+			list = Ln.blk_list;
 		}
 		if (skip)
 			return false;
+		if (list)
+			blk = __ldg(list + blk);
 		const uint32_t elems = (1u << (hbits - mbits)) * static_cast<uint32_t>(colw);
 		const uint32_t bytes = elems * 8u;
 		mbar_expect_tx(&ps.bars[b], bytes);
@@ -1101,8 +1109,8 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	for (int it = 0; w < total; w += gridDim.x, it++)
 	{
 		const int b = it & 1;
-		unsigned int blk, per;
-		const int li = wm_find(wm, w, blk, per);
+		unsigned int bitem, per;
+		const int li = wm_find(wm, w, bitem, per);
 		if (li != ps.lc.li)
 		{
 			__syncthreads();
@@ -1131,6 +1139,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		}
 		if (ps.lc.skip)
 			continue;
+		const unsigned int blk = ps.lc.blk_list ? __ldg(ps.lc.blk_list + bitem) : bitem;
 		const int tbits = ps.lc.tbits, logw = ps.lc.logw, mbits = ps.lc.mbits;
 		const unsigned int rows = 1u << (ps.lc.hbits - mbits);
 		const unsigned int elems = rows << logw;
@@ -1290,7 +1299,7 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			L.blk_e[blk] = best_e;
 		}
 		done++;
-		if (wn >= total || wn >= w - blk + per)
+		if (wn >= total || wn >= w - bitem + per)
 		{
 			__syncthreads();
 			if (tid == 0)
@@ -1343,6 +1352,11 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 	auto issue = [&](long long item, int b) -> bool {
 		unsigned int i, icount;
 		const LatticeDev &Ln = wm_state(states, wm, wm_find(wm, item, i, icount));
+		if (Ln.cblk_list)
+		{
+			const unsigned int pm = (1u << Ln.mbits) - 1u;
+			i = (__ldg(Ln.cblk_list + (i >> Ln.mbits)) << Ln.mbits) | (i & pm);
+		}
 		mbar_expect_tx(&ps.bars[b], kTileElems * 8u);
 		bulk_load(b ? inbuf1 : inbuf0, Ln.m1 + static_cast<size_t>(i) * kTileElems, kTileElems * 8u, &ps.bars[b]);
 		return true;
@@ -1376,7 +1390,7 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 		const int s_g = ps.lc.s_g;
 		const int *tile_scale = ps.lc.tile_scale;
 		u64 *const m2 = ps.lc.m2;
-		const unsigned int cblk = item >> mbits;
+		const unsigned int cblk = ps.lc.cblk_list ? __ldg(ps.lc.cblk_list + (item >> mbits)) : item >> mbits;
 		const unsigned int part = item & ((1u << mbits) - 1u);
 		const unsigned int row0 = part << 11; // first tile row of this chunk
 		const bool timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);

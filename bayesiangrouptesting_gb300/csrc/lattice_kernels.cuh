@@ -120,6 +120,11 @@ struct LatticeDev
 	const double *prior_lo;        // [2^tbits]
 	const double *prior_hi;        // [2^hbits]
 	unsigned long long *ftab;      // k >= 2: BBPA feature masses F_B(E), [2^k][2^n], global scale
+	// k >= 2: BBPA reads the zeta only at the points sum_{v in B} E << (v n),
+	// so K2 visits only the blocks holding them and the middle pass only the
+	// column blocks those need (nullptr: every block).
+	const unsigned int *blk_list;  // K2 block ids, ascending
+	const unsigned int *cblk_list; // middle-pass column blocks, ascending
 	// ---- dynamic (device-updated) ----
 	int mode;                      // K1Mode for the next K1
 	unsigned int pend_e, pend_r;   // pending update

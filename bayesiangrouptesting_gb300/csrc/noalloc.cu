@@ -100,6 +100,8 @@ __global__ void noalloc_setup(const double *posterior, LatticeGeometry g, MapByt
 	L.q_out = nullptr;
 	L.m1 = s.m1;
 	L.m2 = nullptr;
+	L.blk_list = nullptr;
+	L.cblk_list = nullptr;
 	L.tile_total = s.tile_total;
 	L.tile_scale = s.tile_scale;
 	L.blk_score = s.blk_score;

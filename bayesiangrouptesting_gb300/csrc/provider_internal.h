@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 namespace bgt_gpu
 {
@@ -23,6 +24,9 @@ struct CudaFailure : std::runtime_error
 struct LatticeGeometry
 {
 	int n = 0, k = 1, atoms = 0, tbits = 0, hbits = 0, nblk = 1, colw = 1, logw = 0, mbits = 0;
+	// Work items per lattice of K2 and of the middle pass: every block for
+	// k = 1; for k >= 2 only the blocks BBPA reads (bbpa_block_lists).
+	int k2_items = 1, mid_items = 1;
 };
 
 void set_error(const std::string &message);
@@ -42,6 +46,12 @@ LatticeGeometry tuned_geometry(int n, int k, int batch);
 // The dilution response table DilutionTable(n, alpha, h) flattened as
 // [(L - 1) * (n + 1) + r] (dilution.cpp:10-26).
 void dilution_rows(int n, double alpha, double h, double *flat);
+// k >= 2: the K2 blocks that hold the points sum_{v in B} E << (v n) BBPA
+// reads (feature masses, atom masses, the total), ascending, and the column
+// blocks the middle pass must produce for them.
+void bbpa_block_lists(const LatticeGeometry &g, std::vector<unsigned int> &blocks, std::vector<unsigned int> &cblks);
+// The same lists in device memory (nullptr for k = 1); the caller frees both.
+void upload_block_lists(const LatticeGeometry &g, unsigned int **blocks, unsigned int **cblks);
 // Encodes the TMA tensor map through which K1 stores a lattice's zeta partial
 // sums (m1, colw, hbits and nblk must be set); fills m1_map, m1_boxz and
 // m1_stores.  Host-only, allocates nothing.

@@ -467,6 +467,7 @@ struct TreeGraph
 	TreeFlatOut *flat_out = nullptr;
 	double *partials = nullptr;
 	double *d_pi0 = nullptr, *d_dil = nullptr, *d_lo = nullptr, *d_hi = nullptr, *d_thres = nullptr;
+	unsigned int *blk_list = nullptr, *cblk_list = nullptr; // k >= 2: blocks BBPA reads
 	// Pinned inputs and outputs the graph copies from and to.
 	double *h_pi0 = nullptr, *h_dil = nullptr, *h_thres = nullptr, *h_partials = nullptr;
 	LatticeDev *h_root = nullptr;
@@ -485,6 +486,8 @@ struct TreeGraph
 			cudaGraphExecDestroy(exec);
 		for (void *p : allocs)
 			cudaFree(p);
+		cudaFree(blk_list);
+		cudaFree(cblk_list);
 		cudaFreeHost(h_pi0);
 		cudaFreeHost(h_dil);
 		cudaFreeHost(h_thres);
@@ -648,6 +651,9 @@ void build_tree_graph(TreeGraph &t)
 	root.z_norm = 1.0;
 	root.active = t.subjects >= 32 ? 0xFFFFFFFFu : ((1u << t.subjects) - 1u);
 	root.classify_on_update = 1;
+	upload_block_lists(g, &t.blk_list, &t.cblk_list);
+	root.blk_list = t.blk_list;
+	root.cblk_list = t.cblk_list;
 	root.node = t.recs;
 	root.node_stage = 0;
 	root.depth_limit = t.depth;
@@ -852,6 +858,16 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 
 	const unsigned int subject_mask = subjects >= 32 ? 0xFFFFFFFFu : ((1u << subjects) - 1u);
 	const int R = 1 << variants;
+	struct Lists
+	{
+		unsigned int *blocks = nullptr, *cblks = nullptr;
+		~Lists()
+		{
+			cudaFree(blocks);
+			cudaFree(cblks);
+		}
+	} lists;
+	upload_block_lists(g, &lists.blocks, &lists.cblks);
 	std::vector<HostNode> tree(1);
 	Level cur;
 	cur.nodes.push_back(0);
@@ -881,6 +897,8 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 		d.up = up;
 		d.lo = lo;
 		d.classify_on_update = 1;
+		d.blk_list = lists.blocks;
+		d.cblk_list = lists.cblks;
 	}
 	Level prev;
 	for (int depth = 0;; depth++)
