@@ -562,7 +562,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-stages", type=int, default=3, help="stages in the bounded CPU-baseline sample")
-    ap.add_argument("--ref-stages", type=int, default=2, help="stages per core per step in the reference arm")
+    ap.add_argument("--ref-stages", type=int, default=1, help="stages per core per step in the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP64-vs-FP32 n=10 x k=3 measurement")
     ap.add_argument("--no-tree", action="store_true", help="skip the n=20 depth-8 tree measurement")
