@@ -110,7 +110,7 @@ void cuda_check(cudaError_t err, const char *what)
 }
 
 size_t k1_smem_bytes() { return kPipeSmem; }
-size_t k2_smem_bytes(int) { return kPipeSmem; }
+size_t k2_smem_bytes(int) { return kSmemBuf; } // one tile: two CTAs per SM
 
 int sm_count()
 {
@@ -174,7 +174,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	const int per = g.k2_items;
 	const long long items = static_cast<long long>(count) * per;
 	check_items(items);
-	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	const int grid = static_cast<int>(std::min<long long>(items, static_cast<long long>(kK2CtasPerSm) * sm_count()));
 	const WorkMap wm{count, per, nullptr, nullptr};
 	timed_launch(1, stream,
 				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, wm); });
@@ -194,7 +194,7 @@ void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaS
 void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream)
 {
 	check_items(items);
-	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
+	const int grid = static_cast<int>(std::min<long long>(items, static_cast<long long>(kK2CtasPerSm) * sm_count()));
 	timed_launch(1, stream, [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(0), stream>>>(states, wm); });
 	cuda_check(cudaGetLastError(), "k2 launch");
 	count_launches(1);

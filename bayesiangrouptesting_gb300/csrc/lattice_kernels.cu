@@ -1041,11 +1041,14 @@ __device__ __forceinline__ u64 abs_score(u64 m, u64 zg)
 }
 
 // K2: one W-column block of M1 (all 2^h rows, contiguous) per work item.
-__global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *states, WorkMap wm)
+// Two CTAs per SM, one 64 KB tile each: the bulk copy lands in the tile, the
+// zeta transposes run in place, and the next block's copy is issued as soon
+// as the last transpose has read the tile, so it overlaps the scoring, the
+// argmin and the other CTA's work.
+__global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *states, WorkMap wm)
 {
-	u64 *const inbuf0 = tile_u64(0);
-	u64 *const inbuf1 = tile_u64(1);
-	u64 *const work = work_tile();
+	u64 *const tile = tile_u64(0);
+	u64 *const work = tile;
 	int *const shift = g_shift;
 	u64 *const half = g_half;
 	const unsigned int tid = threadIdx.x;
@@ -1061,12 +1064,11 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 	if (tid == 0)
 	{
 		mbar_init(&ps.bars[0], 1);
-		mbar_init(&ps.bars[1], 1);
 		mbar_init_fence();
 		ps.lc.li = -1;
 	}
 	__syncthreads();
-	auto issue = [&](long long item, int b) -> bool {
+	auto issue = [&](long long item) -> bool {
 		unsigned int blk, bcount;
 		const int li = wm_find(wm, item, blk, bcount);
 		int skip, hbits, colw, mbits;
@@ -1097,18 +1099,22 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			blk = __ldg(list + blk);
 		const uint32_t elems = (1u << (hbits - mbits)) * static_cast<uint32_t>(colw);
 		const uint32_t bytes = elems * 8u;
-		mbar_expect_tx(&ps.bars[b], bytes);
-		bulk_load(b ? inbuf1 : inbuf0, src + static_cast<size_t>(blk) * elems, bytes, &ps.bars[b]);
+		mbar_expect_tx(&ps.bars[0], bytes);
+		bulk_load(tile, src + static_cast<size_t>(blk) * elems, bytes, &ps.bars[0]);
 		return true;
 	};
-	uint32_t parity0 = 0u, parity1 = 0u;
-	bool inflight0 = false, inflight1 = false;
+	// Thread 0 issues each copy; every thread tracks whether the current
+	// item's copy was issued (a skipped lattice has none) and the barrier
+	// phase it completes.
+	uint32_t parity = 0u;
+	bool issued = false;
 	if (tid == 0)
-		inflight0 = issue(w, 0);
+		ps.flag = issue(w) ? 1 : 0;
+	__syncthreads();
+	issued = ps.flag != 0;
 	int done = 0;
-	for (int it = 0; w < total; w += gridDim.x, it++)
+	for (; w < total; w += gridDim.x)
 	{
-		const int b = it & 1;
 		unsigned int bitem, per;
 		const int li = wm_find(wm, w, bitem, per);
 		if (li != ps.lc.li)
@@ -1129,16 +1135,16 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			__syncthreads();
 		}
 		const long long wn = w + gridDim.x;
-		if (tid == 0 && wn < total)
-		{
-			proxy_fence();
-			if (b)
-				inflight0 = issue(wn, 0);
-			else
-				inflight1 = issue(wn, 1);
-		}
 		if (ps.lc.skip)
+		{
+			// No copy was issued for this item: the tile is free for the next.
+			__syncthreads();
+			if (tid == 0)
+				ps.flag = (wn < total && issue(wn)) ? 1 : 0;
+			__syncthreads();
+			issued = ps.flag != 0;
 			continue;
+		}
 		const unsigned int blk = ps.lc.blk_list ? __ldg(ps.lc.blk_list + bitem) : bitem;
 		const int tbits = ps.lc.tbits, logw = ps.lc.logw, mbits = ps.lc.mbits;
 		const unsigned int rows = 1u << (ps.lc.hbits - mbits);
@@ -1151,21 +1157,12 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 		const unsigned int active = ps.lc.active;
 		const unsigned int all = ps.lc.n >= 32 ? 0xFFFFFFFFu : ((1u << ps.lc.n) - 1u);
 		const bool want_masses = ps.lc.masses != 0 && ((blk >> ps.lc.mbits) & ((blk >> ps.lc.mbits) - 1u)) == 0;
-		const bool timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);
-		if (b)
-			parity1 ^= 1u;
-		else
-			parity0 ^= 1u;
-		if (tid == 0)
-		{
-			if (b)
-				inflight1 = false;
-			else
-				inflight0 = false;
-		}
+		const bool timed_out = issued && !mbar_wait_bounded(&ps.bars[0], parity);
+		if (issued)
+			parity ^= 1u;
 		// Row bits of the block index y = row * W + column.
 		const unsigned int mask = (rows - 1u) << logw;
-		const u64 *in = b ? inbuf1 : inbuf0;
+		const u64 *in = tile;
 		u64 a[kPerThread];
 #pragma unroll
 		for (int i = 0; i < kPerThread / 2; i++)
@@ -1184,19 +1181,20 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 			a[2 * i + 1] = p.y;
 		}
 		levels_a(a, mask);
-#pragma unroll
-		for (int j = 0; j < kPerThread; j++)
-			work[swz_a(sa, j)] = a[j];
+		// Every thread has read its values from the tile: it becomes the work tile.
 		if (__syncthreads_or(timed_out))
 		{
 			if (tid == 0)
 			{
 				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
-				if (b ? inflight0 : inflight1)
-					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
+				mbar_wait_bounded(&ps.bars[0], parity ^ 1u); // the late copy still targets the tile
 			}
 			return;
 		}
+#pragma unroll
+		for (int j = 0; j < kPerThread; j++)
+			work[swz_a(sa, j)] = a[j];
+		__syncthreads();
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
 			a[j] = work[swz_b(sb, j)];
@@ -1208,6 +1206,13 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 #pragma unroll
 		for (int j = 0; j < kPerThread; j++)
 			a[j] = work[swz_c(sc, j)];
+		// The tile is free: copy the next block while this one is scored.
+		__syncthreads();
+		if (tid == 0)
+		{
+			proxy_fence();
+			ps.flag = (wn < total && issue(wn)) ? 1 : 0;
+		}
 		levels_c(a, mask);
 		// All row bits are done (W >= 4, so y bits 0..1 are column bits).
 		// Score |2 M(E) - Z_g|; within a thread E grows with j, so a strict
@@ -1292,7 +1297,8 @@ __global__ void __launch_bounds__(kThreads, 1) k2_zeta_high_select(LatticeDev *s
 					L.atom_fixed[__ffs(E) - 1] = a[j];
 			}
 		}
-		argmin_block(best, best_e, ps.ws, ps.we);
+		argmin_block(best, best_e, ps.ws, ps.we); // (its barrier also publishes ps.flag)
+		issued = ps.flag != 0;
 		if (tid == 0)
 		{
 			L.blk_score[blk] = best;

@@ -60,6 +60,7 @@ constexpr int kMaxClasses = 32;               // likelihood classes for k = 1 (p
 constexpr int kMaxClassTable = 4096;          // mixed-radix likelihood classes for k >= 2
 constexpr int kSmemBuf = kTileElems * 8;      // one 64 KB tile buffer
 constexpr int kPipeSmem = 3 * kSmemBuf;       // two bulk-copy buffers + one work buffer
+constexpr int kK2CtasPerSm = 2;               // K2 runs two one-tile CTAs per SM
 
 // Modes of K1.
 enum K1Mode : int
