@@ -140,6 +140,26 @@ void configure_kernels()
 	done = true;
 }
 
+// Launch of a persistent pass that may start while the previous kernel of the
+// stream finishes: the pass waits (griddepcontrol.wait) before touching any
+// state, and every pass triggers its dependents when its CTAs reach their
+// last item, so the launch latency between passes overlaps the tail.
+template <typename... Args>
+void launch_pdl(void (*kernel)(Args...), int grid, size_t smem, cudaStream_t stream, Args... args)
+{
+	cudaLaunchConfig_t cfg{};
+	cfg.gridDim = dim3(static_cast<unsigned int>(grid));
+	cfg.blockDim = dim3(kThreads);
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = stream;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	cuda_check(cudaLaunchKernelEx(&cfg, kernel, args...), "pass launch");
+}
+
 // The passes index work items with 32-bit arithmetic.
 void check_items(long long items)
 {
@@ -153,8 +173,7 @@ void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	const WorkMap wm{count, 1 << g.hbits, nullptr, nullptr};
-	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, wm); });
-	cuda_check(cudaGetLastError(), "k1 launch");
+	timed_launch(0, stream, [&] { launch_pdl(k1_zeta_low, grid, k1_smem_bytes(), stream, states, wm); });
 	count_launches(1);
 }
 
@@ -167,8 +186,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 		check_items(mid_items);
 		const int mgrid = static_cast<int>(std::min<long long>(mid_items, sm_count()));
 		const WorkMap wm_mid{count, per_mid, nullptr, nullptr};
-		timed_launch(1, stream, [&] { kmid_zeta<<<mgrid, kThreads, kPipeSmem, stream>>>(states, wm_mid); });
-		cuda_check(cudaGetLastError(), "middle pass launch");
+		timed_launch(1, stream, [&] { launch_pdl(kmid_zeta, mgrid, kPipeSmem, stream, states, wm_mid); });
 		count_launches(1);
 	}
 	const int per = g.k2_items;
@@ -176,9 +194,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, static_cast<long long>(kK2CtasPerSm) * sm_count()));
 	const WorkMap wm{count, per, nullptr, nullptr};
-	timed_launch(1, stream,
-				 [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(g.hbits), stream>>>(states, wm); });
-	cuda_check(cudaGetLastError(), "k2 launch");
+	timed_launch(1, stream, [&] { launch_pdl(k2_zeta_high_select, grid, k2_smem_bytes(g.hbits), stream, states, wm); });
 	count_launches(1);
 }
 
@@ -186,8 +202,7 @@ void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaS
 {
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
-	timed_launch(0, stream, [&] { k1_zeta_low<<<grid, kThreads, k1_smem_bytes(), stream>>>(states, wm); });
-	cuda_check(cudaGetLastError(), "k1 launch");
+	timed_launch(0, stream, [&] { launch_pdl(k1_zeta_low, grid, k1_smem_bytes(), stream, states, wm); });
 	count_launches(1);
 }
 
@@ -195,8 +210,7 @@ void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaS
 {
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, static_cast<long long>(kK2CtasPerSm) * sm_count()));
-	timed_launch(1, stream, [&] { k2_zeta_high_select<<<grid, kThreads, k2_smem_bytes(0), stream>>>(states, wm); });
-	cuda_check(cudaGetLastError(), "k2 launch");
+	timed_launch(1, stream, [&] { launch_pdl(k2_zeta_high_select, grid, k2_smem_bytes(0), stream, states, wm); });
 	count_launches(1);
 }
 

@@ -647,6 +647,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 	double *const inbuf0 = tile_f64(0);
 	double *const inbuf1 = tile_f64(1);
 	const unsigned int tid = threadIdx.x;
+	griddep_wait();
 	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
@@ -722,6 +723,8 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 		const int mode = ps.lc.mode;
 		const long long wn = w + gridDim.x;
 		const long long lat_end = w - r + items; // first item of the next lattice
+		if (wn >= total)
+			griddep_launch_dependents();
 		if (tid == 0)
 		{
 			// Buffer b ^ 1 may still be the source of the previous tile's q'
@@ -1057,6 +1060,7 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 	(void)sb;
 	(void)sc;
 	(void)sd;
+	griddep_wait();
 	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
@@ -1117,6 +1121,8 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 	{
 		unsigned int bitem, per;
 		const int li = wm_find(wm, w, bitem, per);
+		if (w + gridDim.x >= total)
+			griddep_launch_dependents();
 		if (li != ps.lc.li)
 		{
 			__syncthreads();
@@ -1343,6 +1349,7 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 	(void)sb;
 	(void)sc;
 	(void)sd;
+	griddep_wait();
 	const long long total = wm_total(wm);
 	long long w = blockIdx.x;
 	if (w >= total)
@@ -1376,6 +1383,8 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 		const int b = it & 1;
 		unsigned int item, items;
 		const int li = wm_find(wm, w, item, items);
+		if (w + gridDim.x >= total)
+			griddep_launch_dependents();
 		if (li != ps.lc.li)
 		{
 			__syncthreads();

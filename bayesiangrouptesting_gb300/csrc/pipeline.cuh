@@ -96,6 +96,14 @@ __device__ __forceinline__ void st_global_v4_u64(unsigned long long *p, unsigned
 	asm volatile("st.global.v4.u64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(a), "l"(b), "l"(c), "l"(d) : "memory");
 }
 
+// Programmatic dependent launch.  griddep_wait: until the previous kernel of
+// the stream has completed and its writes are visible (a no-op when the
+// launch has no programmatic dependency).  griddep_launch_dependents: this
+// CTA has started its last work item, so the next kernel may be launched
+// (its CTAs then wait in griddep_wait).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
 	uint32_t ok;
