@@ -50,7 +50,8 @@ def test_reference_parity_cases(gpu, oracle, case):
     _check(got, want)
 
 
-@pytest.mark.parametrize("n,depth,dil", [(8, 5, False), (10, 6, True), (12, 4, False), (16, 4, False)])
+@pytest.mark.parametrize("n,depth,dil", [(8, 5, False), (10, 6, True), (12, 4, False), (16, 4, False),
+                                         (5, 17, False)])  # 2^17 slots: the host-driven level loop
 def test_seeded_trees(gpu, oracle, n, depth, dil):
     rng = np.random.default_rng(100 + n)
     pi0 = rng.uniform(0.01, 0.20, n)
@@ -69,6 +70,8 @@ def test_seeded_trees(gpu, oracle, n, depth, dil):
     # seeded
     (True, 4, 2, [0.03, 0.08, 0.05, 0.1, 0.02, 0.07, 0.04, 0.09], 4, 0.01, 0.0, 0),
     (False, 4, 3, [0.02, 0.05, 0.08, 0.03, 0.06, 0.09, 0.04, 0.07, 0.1, 0.05, 0.02, 0.06], 3, 0.01, 0.0, 0),
+    # 4^8 slots exceed the complete layout of the device-built tree: the host-driven level loop
+    (False, 2, 2, [0.05, 0.1, 0.2, 0.3], 8, 0.05, 0.0, 0),
 ])
 def test_multinomial_trees(gpu, oracle, case):
     dil, n, k, pi0, depth, thr, branch, sel = case
