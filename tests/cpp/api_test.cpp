@@ -1,0 +1,159 @@
+// The C++20 host API (include/bgt_gb300/bgt.hpp) against the reference's own
+// C++ pins: tests/cpp/unit/lattice_api_test.cpp:63-99 (public order, upset
+// masses, selections, update, classification, multinomial BBPA = brute
+// force), tests/cpp/unit/dilution_test.cpp:11-13 (table rows) and the
+// single-subject TreeStats golden of tests/cpp/support/assertions.hpp:80-92.
+// Exit status 0 = pass; prints "skip" without a device.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "bgt_gb300/bgt.hpp"
+
+namespace
+{
+
+int failures = 0;
+
+void expect_near(double got, double want, double tol, const char *what)
+{
+	if (!(std::fabs(got - want) <= tol))
+	{
+		std::printf("FAIL %s: got %.17g want %.17g\n", what, got, want);
+		failures++;
+	}
+}
+
+void expect_equal(long long got, long long want, const char *what)
+{
+	if (got != want)
+	{
+		std::printf("FAIL %s: got %lld want %lld\n", what, got, want);
+		failures++;
+	}
+}
+
+template <typename F>
+void expect_error(F &&f, bgt::StatusCode code, const char *what)
+{
+	try
+	{
+		f();
+		std::printf("FAIL %s: no error\n", what);
+		failures++;
+	}
+	catch (const bgt::Error &e)
+	{
+		if (e.code() != code)
+		{
+			std::printf("FAIL %s: status %d\n", what, static_cast<int>(e.code()));
+			failures++;
+		}
+	}
+}
+
+// Exhaustive BBPA for a k-variant lattice: for each experiment, the masses of
+// the 2^k response buckets (bit v set when the pool holds a positive of
+// variant v) and the score sum |mass - 1/2^k|; lowest experiment on ties.
+bgt::state_t brute_force_bbpa(const bgt::Lattice &lat, int n, int k)
+{
+	const int states = 1 << (n * k);
+	std::vector<double> post(static_cast<std::size_t>(states));
+	for (int s = 0; s < states; s++)
+		post[static_cast<std::size_t>(s)] = lat.posterior_probability(static_cast<bgt::state_t>(s));
+	double best = 1e300;
+	bgt::state_t best_e = 0;
+	for (int e = 0; e < (1 << n); e++)
+	{
+		std::vector<double> mass(static_cast<std::size_t>(1) << k, 0.0);
+		for (int s = 0; s < states; s++)
+		{
+			int r = 0;
+			for (int v = 0; v < k; v++)
+				if ((e & ~((s >> (n * v)) & ((1 << n) - 1))) != 0)
+					r |= 1 << v;
+			mass[static_cast<std::size_t>(r)] += post[static_cast<std::size_t>(s)];
+		}
+		double score = 0.0;
+		for (double m : mass)
+			score += std::fabs(m - 1.0 / static_cast<double>(mass.size()));
+		if (score < best)
+		{
+			best = score;
+			best_e = static_cast<bgt::state_t>(e);
+		}
+	}
+	return best_e;
+}
+
+} // namespace
+
+int main()
+{
+	if (!bgt::cuda_available())
+	{
+		std::printf("skip\n");
+		return 0;
+	}
+	const std::vector<double> prior{0.2, 0.4};
+	bgt::Lattice lattice(bgt::LatticeType::replicated_non_dilution, 2, prior);
+	expect_near(lattice.posterior_probability(0), 0.08, 1e-12, "prior state 0");
+	expect_near(lattice.posterior_probability(1), 0.12, 1e-12, "prior state 1");
+	expect_near(lattice.posterior_probability(2), 0.32, 1e-12, "prior state 2");
+	expect_near(lattice.posterior_probability(3), 0.48, 1e-12, "prior state 3");
+	expect_near(lattice.upset_probability_mass(1), 0.60, 1e-12, "upset mass 1");
+	expect_near(lattice.upset_probability_mass(2), 0.80, 1e-12, "upset mass 2");
+	expect_near(lattice.upset_probability_mass(3), 0.48, 1e-12, "upset mass 3");
+	expect_equal(lattice.select_experiment(), 3, "auto selection");
+	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bha), 3, "Op-BHA selection");
+	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bbpa), 3, "Op-BBPA selection");
+	lattice.update(1, 1);
+	const double den = 0.60 * 0.99 + 0.40 * 0.01;
+	expect_near(lattice.posterior_probability(0), 0.08 * 0.01 / den, 1e-12, "posterior state 0");
+	expect_near(lattice.posterior_probability(1), 0.12 * 0.99 / den, 1e-12, "posterior state 1");
+	expect_near(lattice.posterior_probability(2), 0.32 * 0.01 / den, 1e-12, "posterior state 2");
+	expect_near(lattice.posterior_probability(3), 0.48 * 0.99 / den, 1e-12, "posterior state 3");
+	lattice.update_classification(0.01, 0.01);
+	expect_equal(lattice.positive_classification_mask(), 0, "positive mask");
+	expect_equal(lattice.negative_classification_mask(), 1, "negative mask");
+	expect_equal(lattice.is_classified(), 0, "not classified");
+
+	const std::vector<double> multinomial_prior{0.11, 0.23, 0.31, 0.41, 0.17, 0.29};
+	bgt::Lattice multinomial(bgt::LatticeType::replicated_non_dilution, 3, 2, multinomial_prior);
+	expect_equal(multinomial.select_experiment(bgt::SelectorType::op_bbpa), brute_force_bbpa(multinomial, 3, 2),
+				 "multinomial BBPA = brute force");
+	expect_error([&] { multinomial.select_experiment(bgt::SelectorType::op_bha); }, bgt::StatusCode::unsupported,
+				 "Op-BHA with two variants");
+
+	const bgt::DilutionTable table(2, 0.99, 0.005);
+	expect_near(table.at(1, 0), 0.99, 1e-12, "dilution row 1, 0 positives");
+	expect_near(table.at(1, 1), 0.01, 1e-12, "dilution row 1, 1 positive");
+	expect_near(table.at(2, 1), 1.0 - 0.99 / 1.005, 1e-12, "dilution row 2, 1 positive");
+	bgt::Lattice dil(bgt::LatticeType::replicated_dilution, 2, prior);
+	expect_error([&] { dil.update(1, 1, nullptr); }, bgt::StatusCode::invalid_argument, "dilution update without table");
+	dil.update(3, 0, &table);
+	double total = 0.0;
+	for (bgt::state_t s = 0; s < 4; s++)
+		total += dil.posterior_probability(s);
+	expect_near(total, 1.0, 1e-12, "dilution posterior sums to 1");
+
+	bgt::SimulationConfig cfg;
+	cfg.subjects = 1;
+	cfg.prior = {0.2};
+	cfg.options.search_depth = 1;
+	cfg.options.provider = bgt::Provider::cuda;
+	const bgt::TreeStats st = bgt::run_simulation(cfg).stats;
+	expect_equal(st.total_leaves, 2, "single-subject leaves");
+	expect_near(st.correct_probability, 0.792, 1e-12, "single-subject correct");
+	expect_near(st.incorrect_probability, 0.002, 1e-12, "single-subject incorrect");
+	expect_near(st.false_positive_probability, 0.0, 1e-12, "single-subject false positive");
+	expect_near(st.false_negative_probability, 0.002, 1e-12, "single-subject false negative");
+	expect_near(st.unclassified_probability, 0.206, 1e-12, "single-subject unclassified");
+	expect_near(st.expected_stages, 1.0, 1e-12, "single-subject expected stages");
+	expect_near(st.expected_tests, 1.0, 1e-12, "single-subject expected tests");
+
+	std::printf("%s (%d failures)\n", failures ? "FAIL" : "ok", failures);
+	return failures ? 1 : 0;
+}
