@@ -77,6 +77,19 @@ def session_prior(seed: int, session: int, n: int = SUBJECTS) -> np.ndarray:
     return np.array([PRIOR_LO + (PRIOR_HI - PRIOR_LO) * _uniform(seed, session, 1, i) for i in range(n)])
 
 
+def session_response(dilution: bool, n: int, e: int, s: int, alpha: float, h: float, seed: int, session: int,
+                     stage: int) -> int:
+    """Host copy of bgt_session_sample_response for one binary variant
+    (include/bgt_session_rng.h): bit 0 set = the pool tested negative."""
+    if not dilution:
+        p1 = 0.99 if (e & s) == e else 0.01
+    else:
+        pool = bin(e).count("1")
+        pos = pool - bin(e & s).count("1")
+        p1 = alpha if pos == 0 else 1 - alpha * pos / ((pool - pos) * h + pos)
+    return 1 if _uniform(seed, session, 3, stage * 64) < p1 else 0
+
+
 def session_truth(seed: int, session: int, pi0: np.ndarray) -> int:
     s = 0
     for i, p in enumerate(pi0):
@@ -302,8 +315,9 @@ def run_serving(count: int, fp32: bool = False, plain: bool = True):
     }
     if not plain:
         return summary, served
-    # Plain loop: one session at a time through the device session loop, a
-    # lattice per (n, type) reused by reset.
+    # Plain loop: one session at a time through the device session loop
+    # (stages launched back to back, chunked early exit), a lattice per
+    # (n, type) reused by reset.
     lattices = {}
     for q in reqs:
         key = (q.subjects, q.dilution)
@@ -327,6 +341,31 @@ def run_serving(count: int, fp32: bool = False, plain: bool = True):
         plain_ms[i] = 1e3 * (time.perf_counter() - s0)
         identical &= out["stages"] == served[i].stages and np.array_equal(out["experiments"], served[i].experiments)
     plain_wall = time.perf_counter() - t0
+    # The per-call loop: each stage through the Lattice API from the host
+    # (select_experiment -> response drawn on the host -> update ->
+    # update_classification), one session at a time, as a user of the
+    # reference's bgt::Lattice drives it.
+    api_identical = True
+    tables = {}
+    t0 = time.perf_counter()
+    for i, q in enumerate(reqs):
+        lat = lattices[(q.subjects, q.dilution)]
+        lat.reset(q.prior)
+        if q.dilution and q.subjects not in tables:
+            tables[q.subjects] = bgt.DilutionTable(q.subjects, q.alpha, q.h)
+        table = tables[q.subjects] if q.dilution else None
+        ex = []
+        for st in range(SERVE_STAGES):
+            e_pub = lat.select_experiment(bgt.SelectorType.auto_select)
+            e = bgt.reverse_bits(e_pub, q.subjects)
+            r = session_response(q.dilution, q.subjects, e, q.true_state, q.alpha, q.h, q.seed, q.session, st)
+            lat.update(e_pub, r, table)
+            lat.update_classification(THRESHOLD, THRESHOLD)
+            ex.append(e)
+            if lat.is_classified():
+                break
+        api_identical &= len(ex) == served[i].stages and np.array_equal(np.array(ex, np.uint32), served[i].experiments)
+    api_wall = time.perf_counter() - t0
     lattices.clear()
     total_stages = int(stages.sum())
     plain_stage_lat = plain_ms / np.maximum(stages, 1)
@@ -340,6 +379,10 @@ def run_serving(count: int, fp32: bool = False, plain: bool = True):
                                             "p99": float(np.percentile(plain_stage_lat, 99))}},
         "speedup_vs_plain_loop": plain_wall / served_wall,
         "identical_to_plain_loop": bool(identical),
+        "plain_api_loop": {"sessions_per_s": count / api_wall, "session_stages_per_s": total_stages / api_wall,
+                           "wall_s": api_wall, "identical": bool(api_identical),
+                           "loop": "one session at a time, per-stage Lattice API calls from the host"},
+        "speedup_vs_plain_api_loop": api_wall / served_wall,
     }), served
 
 

@@ -137,3 +137,18 @@ def test_closed_form_upset_masses_match_oracle(oracle):
         best, mass = _closed_form_scores(n, pi0, e0, l_in, l_out)
         np.testing.assert_allclose([mass(x) for x in range(1 << n)], upset, rtol=0, atol=1e-14)
         assert abs(best - abs(2.0 * upset[e] - 1.0)) <= 1e-14
+
+
+def test_host_response_stream_matches_oracle(oracle):
+    # The benchmark's host copy of the response stream (its per-call Lattice
+    # API loop) draws what the device sessions and the oracle draw.
+    import bench
+
+    rng = np.random.default_rng(3)
+    for t in range(500):
+        n = int(rng.integers(2, 20))
+        e, s = int(rng.integers(0, 1 << n)), int(rng.integers(0, 1 << n))
+        dil = bool(rng.integers(0, 2))
+        alpha = 0.01 if dil else 0.99
+        want = oracle.lib.orc_sample_response(1 if dil else 0, n, 1, e, s, alpha, 0.005, 7, t, t % 40)
+        assert bench.session_response(dil, n, e, s, alpha, 0.005, 7, t, t % 40) == want
