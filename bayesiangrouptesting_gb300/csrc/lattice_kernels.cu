@@ -648,8 +648,18 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 	double *const inbuf1 = tile_f64(1);
 	const unsigned int tid = threadIdx.x;
 	griddep_wait();
-	const long long total = wm_total(wm);
-	long long w = blockIdx.x;
+	// Work assignment: a lattice with at least one item per CTA is strided
+	// over the CTAs (neighbouring tiles run together); smaller lattices (and
+	// mixed batches) go in contiguous runs, one per CTA, so that the
+	// per-lattice constants are reloaded only when a run crosses into the
+	// next lattice.  `total` is the end of this CTA's items, `step` the
+	// distance to its next item.
+	const long long all_items = wm_total(wm);
+	const bool runs = wm.per == 0 || static_cast<unsigned int>(wm.per) < gridDim.x;
+	const long long run = (all_items + gridDim.x - 1) / gridDim.x;
+	long long w = runs ? static_cast<long long>(blockIdx.x) * run : static_cast<long long>(blockIdx.x);
+	const long long total = runs ? (all_items < w + run ? all_items : w + run) : all_items;
+	const long long step = runs ? 1 : gridDim.x;
 	if (w >= total)
 		return;
 	if (tid == 0)
@@ -706,7 +716,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 	if (tid == 0)
 		inflight0 = issue(w, 0);
 	int done = 0; // items of the cached lattice finished by this CTA, not yet counted
-	for (int it = 0; w < total; w += gridDim.x, it++)
+	for (int it = 0; w < total; w += step, it++)
 	{
 		const int b = it & 1;
 		unsigned int r, items;
@@ -721,7 +731,7 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 				tensormap_acquire(ps.lc.m1_map);
 		}
 		const int mode = ps.lc.mode;
-		const long long wn = w + gridDim.x;
+		const long long wn = w + step;
 		const long long lat_end = w - r + items; // first item of the next lattice
 		if (wn >= total)
 			griddep_launch_dependents();
@@ -1061,8 +1071,18 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 	(void)sc;
 	(void)sd;
 	griddep_wait();
-	const long long total = wm_total(wm);
-	long long w = blockIdx.x;
+	// Work assignment: a lattice with at least one item per CTA is strided
+	// over the CTAs (neighbouring tiles run together); smaller lattices (and
+	// mixed batches) go in contiguous runs, one per CTA, so that the
+	// per-lattice constants are reloaded only when a run crosses into the
+	// next lattice.  `total` is the end of this CTA's items, `step` the
+	// distance to its next item.
+	const long long all_items = wm_total(wm);
+	const bool runs = wm.per == 0 || static_cast<unsigned int>(wm.per) < gridDim.x;
+	const long long run = (all_items + gridDim.x - 1) / gridDim.x;
+	long long w = runs ? static_cast<long long>(blockIdx.x) * run : static_cast<long long>(blockIdx.x);
+	const long long total = runs ? (all_items < w + run ? all_items : w + run) : all_items;
+	const long long step = runs ? 1 : gridDim.x;
 	if (w >= total)
 		return;
 	if (tid == 0)
@@ -1117,11 +1137,11 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 	__syncthreads();
 	issued = ps.flag != 0;
 	int done = 0;
-	for (; w < total; w += gridDim.x)
+	for (; w < total; w += step)
 	{
 		unsigned int bitem, per;
 		const int li = wm_find(wm, w, bitem, per);
-		if (w + gridDim.x >= total)
+		if (w + step >= total)
 			griddep_launch_dependents();
 		if (li != ps.lc.li)
 		{
@@ -1140,7 +1160,7 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 			}
 			__syncthreads();
 		}
-		const long long wn = w + gridDim.x;
+		const long long wn = w + step;
 		if (ps.lc.skip)
 		{
 			// No copy was issued for this item: the tile is free for the next.
@@ -1350,8 +1370,18 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 	(void)sc;
 	(void)sd;
 	griddep_wait();
-	const long long total = wm_total(wm);
-	long long w = blockIdx.x;
+	// Work assignment: a lattice with at least one item per CTA is strided
+	// over the CTAs (neighbouring tiles run together); smaller lattices (and
+	// mixed batches) go in contiguous runs, one per CTA, so that the
+	// per-lattice constants are reloaded only when a run crosses into the
+	// next lattice.  `total` is the end of this CTA's items, `step` the
+	// distance to its next item.
+	const long long all_items = wm_total(wm);
+	const bool runs = wm.per == 0 || static_cast<unsigned int>(wm.per) < gridDim.x;
+	const long long run = (all_items + gridDim.x - 1) / gridDim.x;
+	long long w = runs ? static_cast<long long>(blockIdx.x) * run : static_cast<long long>(blockIdx.x);
+	const long long total = runs ? (all_items < w + run ? all_items : w + run) : all_items;
+	const long long step = runs ? 1 : gridDim.x;
 	if (w >= total)
 		return;
 	if (tid == 0)
@@ -1378,12 +1408,12 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 	bool inflight0 = false, inflight1 = false;
 	if (tid == 0)
 		inflight0 = issue(w, 0);
-	for (int it = 0; w < total; w += gridDim.x, it++)
+	for (int it = 0; w < total; w += step, it++)
 	{
 		const int b = it & 1;
 		unsigned int item, items;
 		const int li = wm_find(wm, w, item, items);
-		if (w + gridDim.x >= total)
+		if (w + step >= total)
 			griddep_launch_dependents();
 		if (li != ps.lc.li)
 		{
@@ -1391,7 +1421,7 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 			load_lattice_cache(wm_state(states, wm, li), li);
 			__syncthreads();
 		}
-		const long long wn = w + gridDim.x;
+		const long long wn = w + step;
 		if (tid == 0 && wn < total)
 		{
 			proxy_fence();
