@@ -235,6 +235,53 @@ __device__ __forceinline__ u64 *work_tile() { return reinterpret_cast<u64 *>(g_s
 
 // K1 epilogue of lattice L (whole CTA): global scale, exact total, and in
 // tree mode the exact atom marginals and the classification.
+// A leaf's share of the tree statistics at branch threshold 0, from the
+// leaf's own lattice.  The reference sums, over every true state t, the
+// prior of t times the product bp of the edge likelihoods down to the leaf
+// (apply_true_state_helper, tree.cpp:174-199; Tree::parse, tree.cpp:70-111).
+// prior(t) * bp(t) is the leaf's posterior q(t) / Z times the probability P
+// of its response path (the product of the update normalisers on the path,
+// which the node records carry), so each sum is a linear functional of the
+// posterior:
+//   correct   = P q(neg) / Z                       (t equal to the negative mask)
+//   incorrect = P - correct
+//   false pos = P sum_{a not in neg} M_a / |pos|   (popcount(t & ~neg) summed over t)
+//   false neg = P sum_{a in neg} (1 - M_a) / |neg|
+//   unclassified = P (a leaf with an unclassified atom)
+// where M_a is the mass with atom a set (negative), which the epilogue has
+// just summed in fixed point for the classification.  States with bp = 0,
+// the only ones threshold 0 prunes, contribute nothing to any sum.
+__device__ void leaf_contributions(const LatticeDev &L, TreeNodeRec &nd)
+{
+	const double P = nd.path;
+	for (int j = 0; j < 5; j++)
+		nd.stat[j] = 0.0;
+	if (__popc(L.pos | L.neg) != L.atoms)
+	{
+		nd.stat[4] = P;
+		return;
+	}
+	const size_t at = L.neg;
+	const double q_neg = L.fp32 ? static_cast<double>(__ldcg(reinterpret_cast<const float *>(L.q_out) + at))
+								: __ldcg(L.q_out + at);
+	const double correct = P * (q_neg / L.z_norm);
+	nd.stat[0] = correct;
+	nd.stat[1] = P - correct;
+	const double zg = __ull2double_rn(L.z_g);
+	const int npos = __popc(L.pos), nneg = __popc(L.neg);
+	double up = 0.0, down = 0.0;
+	for (int a = 0; a < L.atoms; a++)
+	{
+		const u64 m = L.atom_fixed[a];
+		if ((L.neg >> a) & 1u)
+			down += __ull2double_rn(L.z_g - min(m, L.z_g));
+		else
+			up += __ull2double_rn(m);
+	}
+	nd.stat[2] = npos ? P * (up / zg) / npos : 0.0;
+	nd.stat[3] = nneg ? P * (down / zg) / nneg : 0.0;
+}
+
 __device__ void k1_epilogue(LatticeDev &L, int mode)
 {
 	const int tid = threadIdx.x;
@@ -353,6 +400,10 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 			nd->neg = L.neg;
 			nd->leaf = leaf ? 1 : 0;
 			nd->error = L.error;
+			if (mode == kUpdate)
+				nd->path *= L.z_norm;
+			if (leaf)
+				leaf_contributions(L, *nd);
 		}
 		L.k1_count = 0;
 	}

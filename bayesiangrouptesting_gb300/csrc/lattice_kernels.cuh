@@ -80,6 +80,8 @@ struct TreeNodeRec
 	int leaf;              // classified or at the depth limit
 	int exists;            // 0: the parent is a leaf (or missing)
 	int error;             // the lattice's error code
+	double path;           // probability of the node's response path (the parent's, times this update's normaliser)
+	double stat[5];        // leaf: correct, incorrect, false positive, false negative, unclassified mass
 };
 
 // Host-visible progress of a device-driven session (mapped pinned memory),

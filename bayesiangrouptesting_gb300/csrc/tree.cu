@@ -62,6 +62,7 @@ struct SweepParams
 	const int *count_dev; // when set, the node count lives in device memory
 	const double *thres_dev; // when set, the branch threshold lives in device memory
 	double thres;
+	int leaf_sums; // the node list's leaves carry their contributions: nothing to do at threshold <= 0
 	const double *pi0;
 	const double *dil; // [subjects][subjects + 1]
 	const SweepNode *nodes;
@@ -85,14 +86,16 @@ __device__ __forceinline__ double edge_factor(const SweepParams &p, unsigned int
 
 __global__ void __launch_bounds__(kSweepThreads) tree_sweep(SweepParams p)
 {
-	extern __shared__ SweepNode nodes[];
+	// Every thread of a warp reads the same node at the same time: one
+	// cached global transaction per warp, and no shared memory, so the sweep
+	// runs at full occupancy whatever the tree size.
+	const SweepNode *__restrict__ nodes = p.nodes;
 	if (p.count_dev)
 		p.count = *p.count_dev;
 	if (p.thres_dev)
 		p.thres = *p.thres_dev;
-	for (int i = threadIdx.x; i < p.count; i += blockDim.x)
-		nodes[i] = p.nodes[i];
-	__syncthreads();
+	if (p.leaf_sums && p.thres <= 0.0)
+		return;
 	double acc[7] = {0, 0, 0, 0, 0, 0, 0};
 	const unsigned long long total = 1ull << p.atoms;
 	double lvl[kMaxDepth + 2];
@@ -204,6 +207,7 @@ struct TreeFlatOut
 	int leaves; // leaves among them
 	int error;  // first lattice error seen, or 1 << 20 when the node capacity is exceeded
 	int pad;
+	double stats[7]; // the leaves' contributions summed in preorder (branch threshold 0)
 };
 
 // Fills depth d + 1 from depth d: slot c takes parent c / R's geometry and
@@ -254,11 +258,15 @@ __global__ void tree_expand(const LatticeDev *parents, LatticeDev *children, con
 	nd.leaf = 0;
 	nd.exists = exists ? 1 : 0;
 	nd.error = 0;
+	nd.path = pn.path; // K1 multiplies in this node's normaliser
+	for (int j = 0; j < 5; j++)
+		nd.stat[j] = 0.0;
 	child_nodes[c] = nd;
 }
 
 // Preorder list of the existing nodes (children in response order), with
-// each node's subtree end; one thread.
+// each node's subtree end, and the sum of the leaves' contributions in the
+// same order; one thread.
 __global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off, int depth, int R, int atoms,
 							 SweepNode *out, int capacity, TreeFlatOut *res)
 {
@@ -268,6 +276,15 @@ __global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off
 	long long stack_slot[kMaxDepth + 2];
 	int stack_r[kMaxDepth + 2];
 	int n = 0, leaves = 0, err = 0, top = 0;
+	double st[7] = {0, 0, 0, 0, 0, 0, 0};
+	auto add_leaf = [&](const TreeNodeRec &r) {
+		if (!r.leaf)
+			return;
+		for (int j = 0; j < 5; j++)
+			st[j] += r.stat[j];
+		st[5] += r.stage * r.path;
+		st[6] += r.stage * r.path;
+	};
 	// Root.
 	stack_slot[0] = 0;
 	stack_r[0] = 0;
@@ -285,6 +302,7 @@ __global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off
 		stack_idx[0] = 0;
 		n = 1;
 		leaves += rt.leaf;
+		add_leaf(rt);
 		err = rt.error;
 	}
 	while (top >= 0)
@@ -318,6 +336,7 @@ __global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off
 		sn.classified = __popc(ch.pos | ch.neg) == atoms ? 1 : 0;
 		out[n] = sn;
 		leaves += ch.leaf;
+		add_leaf(ch);
 		if (!err)
 			err = ch.error;
 		top++;
@@ -329,6 +348,8 @@ __global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off
 	res->count = n;
 	res->leaves = leaves;
 	res->error = err;
+	for (int j = 0; j < 7; j++)
+		res->stats[j] = st[j];
 }
 
 namespace
@@ -660,11 +681,9 @@ void build_tree_graph(TreeGraph &t)
 	*t.h_root = root; // thresholds are filled per run
 	TreeNodeRec rr{};
 	rr.exists = 1;
+	rr.path = 1.0;
 	*t.h_rootrec = rr;
-	// Sweep shared memory: the node capacity.
-	cuda_check(cudaFuncSetAttribute(tree_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
-									static_cast<int>(kMaxTreeNodes * sizeof(SweepNode))),
-			   "sweep smem");
+
 }
 
 // The launch sequence of one simulation (captured once, or run directly
@@ -723,11 +742,12 @@ uint64_t enqueue_tree(TreeGraph &t)
 	sp.count_dev = &t.flat_out->count;
 	sp.thres_dev = t.d_thres;
 	sp.thres = 0.0;
+	sp.leaf_sums = 1;
 	sp.pi0 = t.d_pi0;
 	sp.dil = t.d_dil;
 	sp.nodes = t.flat;
 	sp.partials = t.partials;
-	tree_sweep<<<t.sweep_blocks, kSweepThreads, kMaxTreeNodes * sizeof(SweepNode), s>>>(sp);
+	tree_sweep<<<t.sweep_blocks, kSweepThreads, 0, s>>>(sp);
 	cuda_check(cudaGetLastError(), "sweep launch");
 	count_launches(1);
 	kernels++;
@@ -807,9 +827,18 @@ void run_tree_graph(int use_dilution, int subjects, int variants, const double *
 													: (out.error == kErrTimeout ? "a bulk copy did not complete in time"
 																				 : "non-finite posterior value"));
 	double sums[7] = {0, 0, 0, 0, 0, 0, 0};
-	for (int b = 0; b < t->sweep_blocks; b++)
+	if (branch_threshold <= 0.0)
+	{
+		// Threshold 0 prunes nothing that contributes: the leaves' own sums.
 		for (int j = 0; j < 7; j++)
-			sums[j] += t->h_partials[static_cast<size_t>(b) * 7 + j];
+			sums[j] = out.stats[j];
+	}
+	else
+	{
+		for (int b = 0; b < t->sweep_blocks; b++)
+			for (int j = 0; j < 7; j++)
+				sums[j] += t->h_partials[static_cast<size_t>(b) * 7 + j];
+	}
 	stats->total_leaves = out.leaves;
 	stats->correct_probability = sums[0];
 	stats->incorrect_probability = sums[1];
@@ -1026,7 +1055,7 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 	cuda_check(cudaMemcpyAsync(d_nodes.ptr, flat.data(), flat.size() * sizeof(SweepNode), cudaMemcpyHostToDevice,
 							   stream),
 			   "sweep nodes up");
-	SweepParams sp;
+	SweepParams sp{}; // no device-side count or threshold; leaf_sums 0
 	sp.atoms = g.atoms;
 	sp.subjects = subjects;
 	sp.variants = variants;
@@ -1037,13 +1066,7 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 	sp.dil = static_cast<double *>(d_dil.ptr);
 	sp.nodes = static_cast<SweepNode *>(d_nodes.ptr);
 	sp.partials = static_cast<double *>(d_partials.ptr);
-	const size_t smem = flat.size() * sizeof(SweepNode);
-	// The attribute stays at the node capacity (the device-built tree's
-	// captured sweep launches with all of it).
-	cuda_check(cudaFuncSetAttribute(tree_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
-									static_cast<int>(kMaxTreeNodes * sizeof(SweepNode))),
-			   "sweep smem");
-	tree_sweep<<<blocks, kSweepThreads, smem, stream>>>(sp);
+	tree_sweep<<<blocks, kSweepThreads, 0, stream>>>(sp);
 	cuda_check(cudaGetLastError(), "sweep launch");
 	count_launches(1);
 	std::vector<double> partials(static_cast<size_t>(blocks) * 7);

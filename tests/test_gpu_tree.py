@@ -78,3 +78,15 @@ def test_multinomial_trees(gpu, oracle, case):
     got = _run(dil, n, pi0, depth, thr, thr, branch, sel, k=k)
     want = oracle.run_simulation(1 if dil else 0, n, k, pi0, depth, thr, thr, branch, sel)
     _check(got, want)
+
+
+@pytest.mark.parametrize("dil,n,k,depth", [(False, 14, 1, 6), (True, 12, 1, 7), (False, 4, 2, 4)])
+def test_leaf_sums_equal_true_state_sweep(gpu, dil, n, k, depth):
+    # Threshold 0 sums each leaf's contributions from its own lattice; a
+    # positive threshold below every non-zero path probability walks the
+    # tree per true state instead.  Both give the same statistics.
+    rng = np.random.default_rng(7 + n)
+    pi0 = rng.uniform(0.01, 0.15, n * k)
+    leaf = _run(dil, n, pi0, depth, k=k)
+    sweep = _run(dil, n, pi0, depth, branch=1e-300, k=k)
+    _check(leaf, sweep)
