@@ -405,12 +405,24 @@ def run_tree(reps: int = 5):
         t0 = time.perf_counter()
         got = bgt.run_simulation(cfg).stats.as_array()
         times.append(time.perf_counter() - t0)
+    # The same tree with a positive branch threshold below every non-zero
+    # path probability: statistics by the per-true-state sweep instead of
+    # the leaves' own lattices.
+    cfg.options.branch_threshold = 1e-300
+    bgt.run_simulation(cfg)
+    sweep_times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        swept = bgt.run_simulation(cfg).stats.as_array()
+        sweep_times.append(time.perf_counter() - t0)
     t0 = time.perf_counter()
     want = Oracle().run_simulation(0, n, 1, pi0, depth)
     cpu_s = time.perf_counter() - t0
     return {"workload": f"binary non-dilution n={n}, Op-BHA, search depth {depth}, TreeStats over 2^{n} true "
                         "states (device-built tree, one CUDA graph replay)",
             "ms_per_tree": 1e3 * statistics.median(times), "leaves": int(got[0]),
+            "ms_per_tree_true_state_sweep": 1e3 * statistics.median(sweep_times),
+            "max_abs_diff_sweep_vs_leaf_sums": float(np.max(np.abs(swept - got))),
             "cpu_baseline": {"seconds": cpu_s, "cores": 1, "kind": "port", "sample": "the same tree, once"},
             "speedup_vs_cpu": cpu_s / statistics.median(times),
             "max_abs_stats_diff_vs_oracle": float(np.max(np.abs(got - want)))}
