@@ -471,6 +471,50 @@ __device__ __forceinline__ int multinomial_class(const ItemCfg &cfg, unsigned in
 	return idx;
 }
 
+// Likelihood-class kinds of an update: containment (non-dilution), popcount
+// of e & s (dilution), mixed radix over variants (k >= 2).
+constexpr int kClsContained = 0, kClsPopcount = 1, kClsMulti = 2;
+
+// Phase B of a K1 item (a warp reads 32 consecutive values of the tile,
+// conflict-free): read the tile (or generate the prior), apply the update,
+// write q' back for its bulk store; v receives the values, f their scaled
+// FP32 sum, bad whether any is non-finite.
+template <int kMode, typename T, int kCls>
+__device__ __forceinline__ void phase_b(const ItemCfg &cfg, T *in, size_t base, unsigned int tsize, unsigned int tid,
+										T (&v)[kPerThread], float &f, bool &bad)
+{
+	const unsigned int e = cfg.e;
+	const bool full = tsize == kTileElems;
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+	{
+		const unsigned int x = map_b(tid, j);
+		T p = T(0);
+		if (full || x < tsize)
+		{
+			if (kMode == kGenerate)
+				p = static_cast<T>(cfg.phi * cfg.prior_lo[x]);
+			else
+				p = in[x];
+			if (kMode == kUpdate)
+			{
+				const unsigned int s0 = static_cast<unsigned int>(base) | x;
+				if (kCls == kClsMulti)
+					p *= multinomial_factor<T>(multinomial_class(cfg, s0));
+				else if (kCls == kClsPopcount)
+					p *= class_factor<T>(__popc(e & s0));
+				else
+					p *= contained_factor<T>(cfg, (e & s0) == e);
+			}
+			if (kMode != kLoad)
+				in[x] = p; // q', bulk-stored by the caller
+		}
+		v[j] = p;
+		f += approx_scaled_hi(p);
+		bad |= non_finite(p);
+	}
+}
+
 // One K1 work item (tile r of lattice L), specialised on the K1 mode.
 template <int kMode, typename T>
 __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int b, bool abort, u64 &total_out,
@@ -486,44 +530,22 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	(void)sd;
 	const int tbits = cfg.tbits;
 	const unsigned int tsize = 1u << tbits;
-	const unsigned int e = cfg.e;
 	const size_t base = static_cast<size_t>(r) << tbits;
 	T *q_out = reinterpret_cast<T *>(cfg.q_out);
-	const double phi = cfg.phi;
 	// Phase B layout (register bits 6..9; a warp reads 32 consecutive
 	// values of the bulk-copied tile, conflict-free): read the tile (or
 	// generate the prior), apply the update, write q' back for its bulk store.
 	T v[kPerThread];
 	float f = 0.0f;
 	bool bad = false;
-#pragma unroll
-	for (int j = 0; j < kPerThread; j++)
-	{
-		const unsigned int x = map_b(tid, j);
-		T p = T(0);
-		if (x < tsize)
-		{
-			if (kMode == kGenerate)
-				p = static_cast<T>(phi * cfg.prior_lo[x]);
-			else
-				p = in[x];
-			if (kMode == kUpdate)
-			{
-				const unsigned int s0 = static_cast<unsigned int>(base) | x;
-				if (cfg.k > 1)
-					p *= multinomial_factor<T>(multinomial_class(cfg, s0));
-				else if (cfg.dilution_classes)
-					p *= class_factor<T>(__popc(e & s0));
-				else
-					p *= contained_factor<T>(cfg, (e & s0) == e);
-			}
-			if (kMode != kLoad)
-				in[x] = p; // q', bulk-stored by the caller
-		}
-		v[j] = p;
-		f += approx_scaled_hi(p);
-		bad |= non_finite(p);
-	}
+	// One straight-line loop per likelihood-class kind (and without the
+	// bounds test for full tiles).
+	if (kMode == kUpdate && cfg.k > 1)
+		phase_b<kMode, T, kClsMulti>(cfg, in, base, tsize, tid, v, f, bad);
+	else if (kMode == kUpdate && cfg.dilution_classes)
+		phase_b<kMode, T, kClsPopcount>(cfg, in, base, tsize, tid, v, f, bad);
+	else
+		phase_b<kMode, T, kClsContained>(cfg, in, base, tsize, tid, v, f, bad);
 	if (bad)
 		ps.flag = 1;
 	if (kMode != kLoad)
