@@ -145,11 +145,11 @@ void configure_kernels()
 // state, and every pass triggers its dependents when its CTAs reach their
 // last item, so the launch latency between passes overlaps the tail.
 template <typename... Args>
-void launch_pdl(void (*kernel)(Args...), int grid, size_t smem, cudaStream_t stream, Args... args)
+void launch_pdl(void (*kernel)(Args...), int grid, int block, size_t smem, cudaStream_t stream, Args... args)
 {
 	cudaLaunchConfig_t cfg{};
 	cfg.gridDim = dim3(static_cast<unsigned int>(grid));
-	cfg.blockDim = dim3(kThreads);
+	cfg.blockDim = dim3(static_cast<unsigned int>(block));
 	cfg.dynamicSmemBytes = smem;
 	cfg.stream = stream;
 	cudaLaunchAttribute attr[1];
@@ -173,7 +173,7 @@ void launch_k1(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
 	const WorkMap wm{count, 1 << g.hbits, nullptr, nullptr};
-	timed_launch(0, stream, [&] { launch_pdl(k1_zeta_low, grid, k1_smem_bytes(), stream, states, wm); });
+	timed_launch(0, stream, [&] { launch_pdl(k1_zeta_low, grid, kK1Threads, k1_smem_bytes(), stream, states, wm); });
 	count_launches(1);
 }
 
@@ -186,7 +186,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 		check_items(mid_items);
 		const int mgrid = static_cast<int>(std::min<long long>(mid_items, sm_count()));
 		const WorkMap wm_mid{count, per_mid, nullptr, nullptr};
-		timed_launch(1, stream, [&] { launch_pdl(kmid_zeta, mgrid, kPipeSmem, stream, states, wm_mid); });
+		timed_launch(1, stream, [&] { launch_pdl(kmid_zeta, mgrid, kThreads, kPipeSmem, stream, states, wm_mid); });
 		count_launches(1);
 	}
 	const int per = g.k2_items;
@@ -194,7 +194,7 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, static_cast<long long>(kK2CtasPerSm) * sm_count()));
 	const WorkMap wm{count, per, nullptr, nullptr};
-	timed_launch(1, stream, [&] { launch_pdl(k2_zeta_high_select, grid, k2_smem_bytes(g.hbits), stream, states, wm); });
+	timed_launch(1, stream, [&] { launch_pdl(k2_zeta_high_select, grid, kThreads, k2_smem_bytes(g.hbits), stream, states, wm); });
 	count_launches(1);
 }
 
@@ -202,7 +202,7 @@ void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaS
 {
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, sm_count()));
-	timed_launch(0, stream, [&] { launch_pdl(k1_zeta_low, grid, k1_smem_bytes(), stream, states, wm); });
+	timed_launch(0, stream, [&] { launch_pdl(k1_zeta_low, grid, kK1Threads, k1_smem_bytes(), stream, states, wm); });
 	count_launches(1);
 }
 
@@ -210,7 +210,7 @@ void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaS
 {
 	check_items(items);
 	const int grid = static_cast<int>(std::min<long long>(items, static_cast<long long>(kK2CtasPerSm) * sm_count()));
-	timed_launch(1, stream, [&] { launch_pdl(k2_zeta_high_select, grid, k2_smem_bytes(0), stream, states, wm); });
+	timed_launch(1, stream, [&] { launch_pdl(k2_zeta_high_select, grid, kThreads, k2_smem_bytes(0), stream, states, wm); });
 	count_launches(1);
 }
 

@@ -122,21 +122,6 @@ __device__ __forceinline__ void levels_c(u64 (&a)[kPerThread], unsigned int mask
 		reg_level(a, l, 2 + l, mask);
 }
 
-// Block-wide float sum over 512 threads; valid in every thread.  The barrier
-// also votes: `abort` becomes true in every thread if any thread passed true.
-__device__ __forceinline__ float block_sum(float v, float *red, bool &abort)
-{
-	for (int o = 16; o > 0; o >>= 1)
-		v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-	if ((threadIdx.x & 31) == 0)
-		red[threadIdx.x >> 5] = v;
-	abort = __syncthreads_or(abort) != 0;
-	float t = (threadIdx.x & 31) < (kThreads / 32) ? red[threadIdx.x & 31] : 0.0f;
-	for (int o = 16; o > 0; o >>= 1)
-		t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
-	return t;
-}
-
 __device__ __forceinline__ void argmin_warp(u64 &s, unsigned int &e)
 {
 	for (int o = 16; o > 0; o >>= 1)
@@ -197,7 +182,13 @@ struct LatCache
 struct PipeShared
 {
 	uint64_t bars[2];
+	uint64_t upd[2];  // K1: the update warps have finished the tile in buffer x
+	uint64_t freed[2]; // K1: the zeta warps have read the tile in buffer x
 	LatCache lc;
+	LatCache uc;      // K1: the update warps' lattice constants
+	float ufred[2][kK1UpdThreads / 32]; // K1: per-buffer partial sums of the update warps
+	int uscale[2];    // K1: fixed-point scale of the tile in buffer x
+	int ubad[2];      // K1: a non-finite value in the tile in buffer x
 	double ctab[kMaxClasses];
 	float ctab32[kMaxClasses]; // the same factors for FP32 lattices
 	float fred[32];
@@ -231,10 +222,18 @@ __device__ __forceinline__ double *tile_f64(int b) { return reinterpret_cast<dou
 __device__ __forceinline__ u64 *tile_u64(int b) { return reinterpret_cast<u64 *>(g_smem + b * kSmemBuf); }
 __device__ __forceinline__ u64 *work_tile() { return reinterpret_cast<u64 *>(g_smem + 2 * kSmemBuf); }
 
+// K1 is warp-specialised: threads 0 .. kThreads - 1 (the zeta threads) run
+// the fixed-point conversion, the 13-bit zeta, the epilogue and every bulk
+// copy; the kK1UpdThreads threads after them apply the updates one tile
+// ahead.  Each role synchronises on its own named barrier.
+constexpr uint32_t kZetaBar = 1, kUpdBar = 2;
+__device__ __forceinline__ void zsync() { named_sync(kZetaBar, kThreads); }
+__device__ __forceinline__ void usync() { named_sync(kUpdBar, kK1UpdThreads); }
+
 // ------------------------------------------------------------------ K1
 
-// K1 epilogue of lattice L (whole CTA): global scale, exact total, and in
-// tree mode the exact atom marginals and the classification.
+// K1 epilogue of lattice L (the zeta threads): global scale, exact total,
+// and in tree mode the exact atom marginals and the classification.
 // A leaf's share of the tree statistics at branch threshold 0, from the
 // leaf's own lattice.  The reference sums, over every true state t, the
 // prior of t times the product bp of the edge likelihoods down to the leaf
@@ -294,7 +293,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 		zr += __shfl_xor_sync(0xFFFFFFFFu, zr, o);
 	if ((tid & 31) == 0)
 		ps.dred[tid >> 5] = zr;
-	__syncthreads();
+	zsync();
 	if (tid < 32)
 	{
 		double t = tid < kThreads / 32 ? ps.dred[tid] : 0.0;
@@ -303,7 +302,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 		if (tid == 0)
 			ps.dred[0] = t;
 	}
-	__syncthreads();
+	zsync();
 	const double z_real = ps.dred[0];
 	const int ez = static_cast<int>((static_cast<u64>(__double_as_longlong(z_real)) >> 52) & 0x7FF);
 	// Global scale: the total lands below 2^62 and no tile is ever scaled up
@@ -315,7 +314,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 		smin = min(smin, __shfl_xor_sync(0xFFFFFFFFu, smin, o));
 	if ((tid & 31) == 0)
 		ps.we[tid >> 5] = static_cast<unsigned int>(smin);
-	__syncthreads();
+	zsync();
 	for (int ww = 0; ww < kThreads / 32; ww++)
 		smin = min(smin, static_cast<int>(ps.we[ww]));
 	const int s_g = min(1084 - ez, smin);
@@ -324,10 +323,10 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 		zg += shr_round(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
 	for (int o = 16; o > 0; o >>= 1)
 		zg += __shfl_xor_sync(0xFFFFFFFFu, zg, o);
-	__syncthreads();
+	zsync();
 	if ((tid & 31) == 0)
 		ps.ured[tid >> 5] = zg;
-	__syncthreads();
+	zsync();
 	const bool tree_masses = mode == kUpdate && L.classify_on_update;
 	if (tree_masses)
 	{
@@ -359,7 +358,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 				L.atom_fixed[atom] = acc;
 		}
 	}
-	__syncthreads();
+	zsync();
 	if (tid == 0)
 	{
 		u64 t = 0;
@@ -407,7 +406,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 		}
 		L.k1_count = 0;
 	}
-	__syncthreads();
+	zsync();
 }
 
 // The per-lattice values a work item needs, read once into registers (the
@@ -475,52 +474,101 @@ __device__ __forceinline__ int multinomial_class(const ItemCfg &cfg, unsigned in
 // of e & s (dilution), mixed radix over variants (k >= 2).
 constexpr int kClsContained = 0, kClsPopcount = 1, kClsMulti = 2;
 
-// Phase B of a K1 item (a warp reads 32 consecutive values of the tile,
-// conflict-free): read the tile (or generate the prior), apply the update,
-// write q' back for its bulk store; v receives the values, f their scaled
-// FP32 sum, bad whether any is non-finite.
+// The update warps' pass over one tile in shared buffer `in` (thread tu
+// takes elements tu + 128 k: a warp reads 32 consecutive values): generate
+// the prior or apply the update in place (q', bulk-stored by the zeta
+// threads), accumulating the scaled FP32 sum f and the non-finite flag.
+// Load mode only reads.  Batches of 8 values per thread: all loads first,
+// then 8 independent multiplies, so that the two update warps per scheduler
+// keep the FP64 pipe busy.
 template <int kMode, typename T, int kCls>
-__device__ __forceinline__ void phase_b(const ItemCfg &cfg, T *in, size_t base, unsigned int tsize, unsigned int tid,
-										T (&v)[kPerThread], float &f, bool &bad)
+__device__ __forceinline__ void update_tile(const ItemCfg &cfg, T *in, size_t base, unsigned int tsize,
+											unsigned int tu, float &f, bool &bad)
 {
+	constexpr int kBatch = 8;
 	const unsigned int e = cfg.e;
 	const bool full = tsize == kTileElems;
-#pragma unroll
-	for (int j = 0; j < kPerThread; j++)
+	for (int k0 = 0; k0 < kTileElems / kK1UpdThreads; k0 += kBatch)
 	{
-		const unsigned int x = map_b(tid, j);
-		T p = T(0);
-		if (full || x < tsize)
+		if (!full && tu + static_cast<unsigned int>(k0) * kK1UpdThreads >= tsize)
+			break;
+		T p[kBatch], c[kBatch];
+#pragma unroll
+		for (int j = 0; j < kBatch; j++)
 		{
+			const unsigned int x = tu + static_cast<unsigned int>(k0 + j) * kK1UpdThreads;
+			const bool in_tile = full || x < tsize;
 			if (kMode == kGenerate)
-				p = static_cast<T>(cfg.phi * cfg.prior_lo[x]);
-			else
-				p = in[x];
-			if (kMode == kUpdate)
 			{
-				const unsigned int s0 = static_cast<unsigned int>(base) | x;
-				if (kCls == kClsMulti)
-					p *= multinomial_factor<T>(multinomial_class(cfg, s0));
-				else if (kCls == kClsPopcount)
-					p *= class_factor<T>(__popc(e & s0));
-				else
-					p *= contained_factor<T>(cfg, (e & s0) == e);
+				p[j] = in_tile ? static_cast<T>(cfg.phi * cfg.prior_lo[x]) : T(0);
+				c[j] = T(1);
 			}
-			if (kMode != kLoad)
-				in[x] = p; // q', bulk-stored by the caller
+			else
+			{
+				p[j] = in_tile ? in[x] : T(0);
+				const unsigned int s0 = static_cast<unsigned int>(base) | x;
+				if (kMode != kUpdate)
+					c[j] = T(1);
+				else if (kCls == kClsMulti)
+					c[j] = multinomial_factor<T>(multinomial_class(cfg, s0));
+				else if (kCls == kClsPopcount)
+					c[j] = class_factor<T>(__popc(e & s0));
+				else
+					c[j] = contained_factor<T>(cfg, (e & s0) == e);
+			}
 		}
-		v[j] = p;
-		f += approx_scaled_hi(p);
-		bad |= non_finite(p);
+		if (kMode == kUpdate)
+		{
+#pragma unroll
+			for (int j = 0; j < kBatch; j++)
+				p[j] *= c[j];
+		}
+#pragma unroll
+		for (int j = 0; j < kBatch; j++)
+		{
+			const unsigned int x = tu + static_cast<unsigned int>(k0 + j) * kK1UpdThreads;
+			if (full || x < tsize)
+			{
+				if (kMode != kLoad)
+					in[x] = p[j];
+				f += approx_scaled_hi(p[j]);
+				bad |= non_finite(p[j]);
+			}
+		}
 	}
 }
 
-// One K1 work item (tile r of lattice L), specialised on the K1 mode.
+// The same with the likelihood-class kind chosen at run time (uniform per
+// lattice): one straight-line loop per kind.
 template <int kMode, typename T>
-__device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int b, bool abort, u64 &total_out,
-										int &scale_out)
+__device__ __forceinline__ void update_tile_any(const ItemCfg &cfg, T *in, size_t base, unsigned int tsize,
+												unsigned int tu, float &f, bool &bad)
 {
-	T *const in = reinterpret_cast<T *>(tile_f64(b));
+	if (kMode == kUpdate && cfg.k > 1)
+		update_tile<kMode, T, kClsMulti>(cfg, in, base, tsize, tu, f, bad);
+	else if (kMode == kUpdate && cfg.dilution_classes)
+		update_tile<kMode, T, kClsPopcount>(cfg, in, base, tsize, tu, f, bad);
+	else
+		update_tile<kMode, T, kClsContained>(cfg, in, base, tsize, tu, f, bad);
+}
+
+// Tile scale from the summed estimate: the tile total lands in
+// [2^61, 2^62 (1 + 2^-20)).
+__device__ __forceinline__ int tile_scale_of(float est)
+{
+	const int ef = (__float_as_int(est) >> 23) & 0xFF;
+	return ef == 0 ? 238 : 252 - ef;
+}
+
+// The zeta threads' part of one K1 work item (tile r, updated by the update
+// warps in buffer x, with scale `scale`): bulk-store q' (store_q), convert to
+// fixed point, release the buffer (issue2() then starts the copy of the item
+// after next into it), run the 13 zeta levels and store the partial sums.
+template <typename T, typename Issue2>
+__device__ __forceinline__ void zeta_item(const ItemCfg &cfg, unsigned int r, int x, int scale, bool store_q,
+										  Issue2 &&issue2, u64 &total_out)
+{
+	T *const in = reinterpret_cast<T *>(tile_f64(x));
 	u64 *const work = work_tile();
 	const unsigned int tid = threadIdx.x;
 	const unsigned int sa = swz_a_base(tid), sb = swz_b_base(tid), sc = swz_c_base(tid), sd = swz_d_base(tid);
@@ -530,51 +578,39 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	(void)sd;
 	const int tbits = cfg.tbits;
 	const unsigned int tsize = 1u << tbits;
+	const bool full = tsize == kTileElems;
 	const size_t base = static_cast<size_t>(r) << tbits;
-	T *q_out = reinterpret_cast<T *>(cfg.q_out);
-	// Phase B layout (register bits 6..9; a warp reads 32 consecutive
-	// values of the bulk-copied tile, conflict-free): read the tile (or
-	// generate the prior), apply the update, write q' back for its bulk store.
-	T v[kPerThread];
-	float f = 0.0f;
-	bool bad = false;
-	// One straight-line loop per likelihood-class kind (and without the
-	// bounds test for full tiles).
-	if (kMode == kUpdate && cfg.k > 1)
-		phase_b<kMode, T, kClsMulti>(cfg, in, base, tsize, tid, v, f, bad);
-	else if (kMode == kUpdate && cfg.dilution_classes)
-		phase_b<kMode, T, kClsPopcount>(cfg, in, base, tsize, tid, v, f, bad);
-	else
-		phase_b<kMode, T, kClsContained>(cfg, in, base, tsize, tid, v, f, bad);
-	if (bad)
-		ps.flag = 1;
-	if (kMode != kLoad)
-		proxy_fence(); // q' in shared memory -> visible to the bulk store
-	// The previous tile's zeta-partial-sum stores read the work tile, which
-	// this tile writes after the next barrier.
-	if (threadIdx.x == 0)
-		bulk_wait_read_all();
-	const float est = block_sum(f, ps.fred, abort);
-	if (abort)
-		return true;
-	if (kMode != kLoad && threadIdx.x == 0)
+	if (store_q && tid == 0)
 	{
-		bulk_store(q_out + base, in, static_cast<uint32_t>(sizeof(T)) << tbits);
+		bulk_store(reinterpret_cast<T *>(cfg.q_out) + base, in, static_cast<uint32_t>(sizeof(T)) << tbits);
 		bulk_commit();
 	}
-	// Scale so that the tile total lands in [2^61, 2^62 (1 + 2^-20)).
-	const int ef = (__float_as_int(est) >> 23) & 0xFF;
-	const int scale = ef == 0 ? 238 : 252 - ef;
+	// Phase B layout (register bits 6..9; a warp reads 32 consecutive
+	// values, conflict-free).
 	u64 a[kPerThread];
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
-		a[j] = to_fixed_fast(v[j], scale);
+	{
+		const unsigned int xx = map_b(tid, j);
+		a[j] = (full || xx < tsize) ? to_fixed_fast(in[xx], scale) : 0ull;
+	}
 	const unsigned int mask = tsize - 1u;
 	levels_b(a, mask);
+	// q' and the previous item's partial sums (the work tile) have left
+	// shared memory; after the barrier no zeta thread reads buffer x again.
+	if (tid == 0)
+		bulk_wait_read_all();
+	zsync();
+	if (tid == 0)
+	{
+		mbar_arrive(&ps.freed[x]);
+		proxy_fence();
+		issue2();
+	}
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
 		work[swz_b(sb, j)] = a[j];
-	__syncthreads();
+	zsync();
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
 		a[j] = work[swz_c(sc, j)];
@@ -593,7 +629,7 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
 		work[swz_c(sc, j)] = a[j];
-	__syncthreads();
+	zsync();
 #pragma unroll
 	for (int j = 0; j < kPerThread; j++)
 		a[j] = work[swz_a(sa, j)];
@@ -601,13 +637,13 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 	// The finished tile, in column order (pairs: conflict-free), is stored to
 	// m1 by the tensor map: column block c of row r lands at
 	// m1[(c * 2^hbits + r) * W].
-	__syncthreads();
+	zsync();
 #pragma unroll
 	for (int i = 0; i < kPerThread / 2; i++)
 		*reinterpret_cast<ulonglong2 *>(work + map_a(tid, 2 * i)) = make_ulonglong2(a[2 * i], a[2 * i + 1]);
 	proxy_fence();
-	__syncthreads();
-	if (threadIdx.x == 0)
+	zsync();
+	if (tid == 0)
 	{
 		const int step = cfg.m1_boxz * cfg.colw;
 		for (int k = 0; k < cfg.m1_stores; k++)
@@ -615,15 +651,13 @@ __device__ __forceinline__ bool k1_item(const ItemCfg &cfg, unsigned int r, int 
 		bulk_commit();
 	}
 	total_out = a[0]; // element 0 of the finished tile: the tile total
-	scale_out = scale;
-	return false;
 }
 
 // Loads the per-lattice constants of lattice li into ps.lc (warp 0), the
 // likelihood-class table included for updates.
 // K1 only (the table lives in K1's shared memory): the multinomial class
 // table of lattice L's pending update, filled by all threads.
-__device__ __forceinline__ void load_class_table(const LatticeDev &L)
+__device__ __forceinline__ void load_class_table(const LatticeDev &L, unsigned int first, unsigned int stride)
 {
 	const int k = L.k;
 	if (k < 2 || L.mode != kUpdate)
@@ -635,7 +669,7 @@ __device__ __forceinline__ void load_class_table(const LatticeDev &L)
 	for (int v = 0; v < k; v++)
 		entries *= radix;
 	const double z = L.z_norm;
-	for (int idx = threadIdx.x; idx < entries && idx < kMaxClassTable; idx += kThreads)
+	for (int idx = static_cast<int>(first); idx < entries && idx < kMaxClassTable; idx += static_cast<int>(stride))
 	{
 		double f = 1.0;
 		int rest = idx;
@@ -654,17 +688,19 @@ __device__ __forceinline__ void load_class_table(const LatticeDev &L)
 	}
 }
 
-__device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
+// Fills cache c with lattice li's constants (one warp; lane = the lane
+// index); with_ctab also fills the binary update factors ps.ctab.
+__device__ __forceinline__ void fill_lattice_cache(const LatticeDev &L, int li, LatCache &c, unsigned int lane,
+												   bool with_ctab)
 {
-	const unsigned int tid = threadIdx.x;
+	const unsigned int tid = lane;
 	const int mode = L.mode;
 	const unsigned int e = L.pend_e;
 	const int k = L.k;
 	const int pool = __popc(e);
 	const int radix = L.dilution ? pool + 1 : 2;
-	if (tid < 32)
 	{
-		if (mode == kUpdate && k == 1)
+		if (with_ctab && mode == kUpdate && k == 1)
 		{
 			ps.ctab[tid] = static_cast<int>(tid) <= pool
 							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1) / L.z_norm
@@ -674,7 +710,6 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 		__syncwarp();
 		if (tid == 0)
 		{
-			LatCache &c = ps.lc;
 			c.li = li;
 			c.mode = mode;
 			c.e = e;
@@ -707,50 +742,178 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 			c.tile_total = L.tile_total;
 			c.tile_scale = L.tile_scale;
 			c.ftab = L.ftab;
-			c.c_in = mode == kUpdate && k == 1 ? ps.ctab[pool] : 0.0;
-			c.c_out = mode == kUpdate && k == 1 ? ps.ctab[0] : 0.0;
+			c.c_in = with_ctab && mode == kUpdate && k == 1 ? ps.ctab[pool] : 0.0;
+			c.c_out = with_ctab && mode == kUpdate && k == 1 ? ps.ctab[0] : 0.0;
 		}
 	}
 }
 
-// K1: [update] -> per-tile fixed point -> zeta over the low t bits -> M1.
-// Grid: persistent, at most one CTA per work item; an item is one tile.
-__global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, WorkMap wm)
+// K2 and the middle pass: warp 0 loads ps.lc.
+__device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
+{
+	if (threadIdx.x < 32)
+		fill_lattice_cache(L, li, ps.lc, threadIdx.x, true);
+}
+
+// The per-item constants from a lattice cache.
+__device__ __forceinline__ ItemCfg item_cfg(const LatCache &c, unsigned int r)
+{
+	ItemCfg cfg;
+	cfg.q_out = c.q_out;
+	cfg.m1 = c.m1;
+	cfg.prior_lo = c.prior_lo;
+	cfg.phi = c.mode == kGenerate ? c.prior_hi[r] : 0.0;
+	cfg.e = c.e;
+	cfg.tbits = c.tbits;
+	cfg.hbits = c.hbits;
+	cfg.colw = c.colw;
+	cfg.logw = c.logw;
+	cfg.dilution_classes = c.dilution;
+	cfg.c_in = c.c_in;
+	cfg.c_out = c.c_out;
+	cfg.c_in32 = static_cast<float>(c.c_in);
+	cfg.c_out32 = static_cast<float>(c.c_out);
+	cfg.m1_map = c.m1_map;
+	cfg.m1_boxz = c.m1_boxz;
+	cfg.m1_stores = c.m1_stores;
+	cfg.k = c.k;
+	cfg.n = c.n;
+	cfg.radix = c.radix;
+	return cfg;
+}
+
+// Work assignment of the persistent passes: a lattice with at least one
+// item per CTA is strided over the CTAs (neighbouring tiles run together);
+// smaller lattices (and mixed batches) go in contiguous runs, one per CTA, so
+// that the per-lattice constants are reloaded only when a run crosses into
+// the next lattice.  w is this CTA's first item, total the end of its items,
+// step the distance to its next item.
+struct ItemRange
+{
+	long long w, total, step;
+};
+__device__ __forceinline__ ItemRange item_range(const WorkMap &wm)
+{
+	const long long all_items = wm_total(wm);
+	const bool runs = wm.per == 0 || static_cast<unsigned int>(wm.per) < gridDim.x;
+	const long long run = (all_items + gridDim.x - 1) / gridDim.x;
+	ItemRange ir;
+	ir.w = runs ? static_cast<long long>(blockIdx.x) * run : static_cast<long long>(blockIdx.x);
+	ir.total = runs ? (all_items < ir.w + run ? all_items : ir.w + run) : all_items;
+	ir.step = runs ? 1 : gridDim.x;
+	return ir;
+}
+
+// K1's update warps: for each item of the CTA (buffer x = item parity), wait
+// until the zeta threads have released x and its copy has landed, update the
+// tile in place, and hand it over with its scale (ps.upd[x]).
+__device__ void k1_update_role(LatticeDev *states, const WorkMap &wm, ItemRange ir)
+{
+	const unsigned int tu = threadIdx.x - kThreads;
+	uint32_t pfree0 = 0u, pfree1 = 0u, pfull0 = 0u, pfull1 = 0u;
+	bool used0 = false, used1 = false;
+	for (int it = 0; ir.w < ir.total; ir.w += ir.step, it++)
+	{
+		const int x = it & 1;
+		unsigned int r, items;
+		const int li = wm_find(wm, ir.w, r, items);
+		if (li != ps.uc.li)
+		{
+			usync();
+			const LatticeDev &L = wm_state(states, wm, li);
+			if (tu < 32)
+				fill_lattice_cache(L, li, ps.uc, tu, true);
+			load_class_table(L, tu, kK1UpdThreads);
+			usync();
+		}
+		if (ps.uc.skip)
+			continue; // no copy, no hand-over: the zeta threads skip it too
+		const int mode = ps.uc.mode;
+		bool late = false;
+		if (x ? used1 : used0)
+		{
+			late |= !mbar_wait_bounded(&ps.freed[x], x ? pfree1 : pfree0);
+			if (x)
+				pfree1 ^= 1u;
+			else
+				pfree0 ^= 1u;
+		}
+		if (x)
+			used1 = true;
+		else
+			used0 = true;
+		if (mode != kGenerate)
+		{
+			late |= !mbar_wait_bounded(&ps.bars[x], x ? pfull1 : pfull0);
+			if (x)
+				pfull1 ^= 1u;
+			else
+				pfull0 ^= 1u;
+		}
+		if (named_sync_or(kUpdBar, kK1UpdThreads, late))
+		{
+			if (tu == 0)
+			{
+				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
+				ps.abort = 1;
+				mbar_arrive(&ps.upd[x]);
+			}
+			return;
+		}
+		const ItemCfg cfg = item_cfg(ps.uc, r);
+		const unsigned int tsize = 1u << cfg.tbits;
+		const size_t base = static_cast<size_t>(r) << cfg.tbits;
+		float f = 0.0f;
+		bool bad = false;
+		if (ps.uc.fp32)
+		{
+			float *in = reinterpret_cast<float *>(tile_f64(x));
+			if (mode == kUpdate)
+				update_tile_any<kUpdate, float>(cfg, in, base, tsize, tu, f, bad);
+			else if (mode == kGenerate)
+				update_tile_any<kGenerate, float>(cfg, in, base, tsize, tu, f, bad);
+			else
+				update_tile_any<kLoad, float>(cfg, in, base, tsize, tu, f, bad);
+		}
+		else
+		{
+			double *in = tile_f64(x);
+			if (mode == kUpdate)
+				update_tile_any<kUpdate, double>(cfg, in, base, tsize, tu, f, bad);
+			else if (mode == kGenerate)
+				update_tile_any<kGenerate, double>(cfg, in, base, tsize, tu, f, bad);
+			else
+				update_tile_any<kLoad, double>(cfg, in, base, tsize, tu, f, bad);
+		}
+		if (mode != kLoad)
+			proxy_fence(); // q' in shared memory -> visible to its bulk store
+		for (int o = 16; o > 0; o >>= 1)
+			f += __shfl_xor_sync(0xFFFFFFFFu, f, o);
+		if ((tu & 31u) == 0)
+			ps.ufred[x][tu >> 5] = f;
+		bad = named_sync_or(kUpdBar, kK1UpdThreads, bad);
+		if (tu == 0)
+		{
+			float est = 0.0f;
+			for (int wi = 0; wi < kK1UpdThreads / 32; wi++)
+				est += ps.ufred[x][wi];
+			ps.uscale[x] = tile_scale_of(est);
+			ps.ubad[x] = bad ? 1 : 0;
+			mbar_arrive(&ps.upd[x]);
+		}
+	}
+}
+
+// K1's zeta threads: for each item, take the updated tile from buffer x,
+// run the zeta, issue every bulk copy, count finished lattices and run their
+// epilogues.
+__device__ void k1_zeta_role(LatticeDev *states, const WorkMap &wm, ItemRange ir)
 {
 	double *const inbuf0 = tile_f64(0);
 	double *const inbuf1 = tile_f64(1);
 	const unsigned int tid = threadIdx.x;
-	griddep_wait();
-	// Work assignment: a lattice with at least one item per CTA is strided
-	// over the CTAs (neighbouring tiles run together); smaller lattices (and
-	// mixed batches) go in contiguous runs, one per CTA, so that the
-	// per-lattice constants are reloaded only when a run crosses into the
-	// next lattice.  `total` is the end of this CTA's items, `step` the
-	// distance to its next item.
-	const long long all_items = wm_total(wm);
-	const bool runs = wm.per == 0 || static_cast<unsigned int>(wm.per) < gridDim.x;
-	const long long run = (all_items + gridDim.x - 1) / gridDim.x;
-	long long w = runs ? static_cast<long long>(blockIdx.x) * run : static_cast<long long>(blockIdx.x);
-	const long long total = runs ? (all_items < w + run ? all_items : w + run) : all_items;
-	const long long step = runs ? 1 : gridDim.x;
-	if (w >= total)
-		return;
-	if (tid == 0)
-	{
-		mbar_init(&ps.bars[0], 1);
-		mbar_init(&ps.bars[1], 1);
-		mbar_init_fence();
-		ps.flag = 0;
-	}
-	{
-		unsigned int i0, n0;
-		const int l0 = wm_find(wm, w, i0, n0);
-		load_lattice_cache(wm_state(states, wm, l0), l0);
-		load_class_table(wm_state(states, wm, l0));
-	}
-	__syncthreads();
-	if (tid == 0)
-		tensormap_acquire(ps.lc.m1_map);
+	const long long total = ir.total, step = ir.step;
+	long long w = ir.w;
 	// Thread 0 issues the bulk copy of item `item` into buffer b (no copy
 	// for generated priors or skipped lattices); same-lattice items use the
 	// cached constants.
@@ -784,120 +947,91 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 				  &ps.bars[b]);
 		return true;
 	};
-	uint32_t parity0 = 0u, parity1 = 0u;
-	bool inflight0 = false, inflight1 = false; // meaningful in thread 0 only
+	uint32_t pupd0 = 0u, pupd1 = 0u;
+	unsigned int issued0 = 0u, issued1 = 0u; // copies issued into each buffer (thread 0)
 	if (tid == 0)
-		inflight0 = issue(w, 0);
-	int done = 0; // items of the cached lattice finished by this CTA, not yet counted
+	{
+		issued0 += issue(w, 0) ? 1u : 0u;
+		if (w + step < total)
+			issued1 += issue(w + step, 1) ? 1u : 0u;
+	}
+	int done = 0;    // items of the cached lattice finished by this CTA, not yet counted
+	bool lat_bad = false; // thread 0: a non-finite value in the cached lattice
 	for (int it = 0; w < total; w += step, it++)
 	{
-		const int b = it & 1;
+		const int x = it & 1;
 		unsigned int r, items;
 		const int li = wm_find(wm, w, r, items);
 		if (li != ps.lc.li)
 		{
-			__syncthreads();
-			load_lattice_cache(wm_state(states, wm, li), li);
-			load_class_table(wm_state(states, wm, li));
-			__syncthreads();
+			zsync();
+			if (tid < 32)
+				fill_lattice_cache(wm_state(states, wm, li), li, ps.lc, tid, false);
+			zsync();
 			if (tid == 0)
 				tensormap_acquire(ps.lc.m1_map);
 		}
 		const int mode = ps.lc.mode;
 		const long long wn = w + step;
+		const long long wn2 = wn + step;
 		const long long lat_end = w - r + items; // first item of the next lattice
 		if (wn >= total)
 			griddep_launch_dependents();
-		if (tid == 0)
+		auto issue2 = [&]() {
+			if (wn2 < total)
+			{
+				const unsigned int n = issue(wn2, x) ? 1u : 0u;
+				if (x)
+					issued1 += n;
+				else
+					issued0 += n;
+			}
+		};
+		if (ps.lc.skip)
 		{
-			// Buffer b ^ 1 may still be the source of the previous tile's q'
-			// bulk store; the newest group (its zeta-partial-sum stores, from
-			// the work tile) may run on.
-			bulk_wait_read_all_but_last();
-			if (wn < total)
+			// A finished session: no copy, no update; its buffer takes the
+			// copy of the item after next.
+			if (tid == 0)
 			{
 				proxy_fence();
-				if (b)
-					inflight0 = issue(wn, 0);
-				else
-					inflight1 = issue(wn, 1);
+				issue2();
 			}
+			continue;
 		}
-		if (ps.lc.skip)
-			continue; // a finished session: no copy was issued for it
-		bool timed_out = false;
-		if (mode != kGenerate)
-		{
-			timed_out = !mbar_wait_bounded(&ps.bars[b], b ? parity1 : parity0);
-			if (b)
-				parity1 ^= 1u;
-			else
-				parity0 ^= 1u;
-		}
-		if (tid == 0)
-		{
-			if (b)
-				inflight1 = false;
-			else
-				inflight0 = false;
-		}
-		ItemCfg cfg;
-		cfg.q_out = ps.lc.q_out;
-		cfg.m1 = ps.lc.m1;
-		cfg.prior_lo = ps.lc.prior_lo;
-		cfg.phi = mode == kGenerate ? ps.lc.prior_hi[r] : 0.0;
-		cfg.e = ps.lc.e;
-		cfg.tbits = ps.lc.tbits;
-		cfg.hbits = ps.lc.hbits;
-		cfg.colw = ps.lc.colw;
-		cfg.logw = ps.lc.logw;
-		cfg.dilution_classes = ps.lc.dilution;
-		cfg.c_in = ps.lc.c_in;
-		cfg.c_out = ps.lc.c_out;
-		cfg.c_in32 = static_cast<float>(ps.lc.c_in);
-		cfg.c_out32 = static_cast<float>(ps.lc.c_out);
-		cfg.m1_map = ps.lc.m1_map;
-		cfg.m1_boxz = ps.lc.m1_boxz;
-		cfg.m1_stores = ps.lc.m1_stores;
-		cfg.k = ps.lc.k;
-		cfg.n = ps.lc.n;
-		cfg.radix = ps.lc.radix;
-		u64 tile_total = 0;
-		int tile_scale = 0;
-		bool abort;
-		if (ps.lc.fp32)
-		{
-			if (mode == kUpdate)
-				abort = k1_item<kUpdate, float>(cfg, r, b, timed_out, tile_total, tile_scale);
-			else if (mode == kGenerate)
-				abort = k1_item<kGenerate, float>(cfg, r, b, timed_out, tile_total, tile_scale);
-			else
-				abort = k1_item<kLoad, float>(cfg, r, b, timed_out, tile_total, tile_scale);
-		}
+		bool late = !mbar_wait_bounded(&ps.upd[x], x ? pupd1 : pupd0);
+		if (x)
+			pupd1 ^= 1u;
 		else
-		{
-			if (mode == kUpdate)
-				abort = k1_item<kUpdate, double>(cfg, r, b, timed_out, tile_total, tile_scale);
-			else if (mode == kGenerate)
-				abort = k1_item<kGenerate, double>(cfg, r, b, timed_out, tile_total, tile_scale);
-			else
-				abort = k1_item<kLoad, double>(cfg, r, b, timed_out, tile_total, tile_scale);
-		}
-		if (abort)
+			pupd0 ^= 1u;
+		if (named_sync_or(kZetaBar, kThreads, late || ps.abort != 0))
 		{
 			if (tid == 0)
 			{
 				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
-				if (b ? inflight0 : inflight1)
-					mbar_wait_bounded(&ps.bars[b ^ 1], b ? parity0 : parity1);
+				ps.abort = 1;
+				// Copies still in flight target this CTA's shared memory
+				// (at most one per buffer).
+				if (issued0)
+					mbar_wait_bounded(&ps.bars[0], (issued0 - 1u) & 1u);
+				if (issued1)
+					mbar_wait_bounded(&ps.bars[1], (issued1 - 1u) & 1u);
 				bulk_wait_all();
 			}
 			return;
 		}
+		const int scale = ps.uscale[x];
+		if (tid == 0 && ps.ubad[x])
+			lat_bad = true;
+		ItemCfg cfg = item_cfg(ps.lc, r);
+		u64 tile_total = 0;
+		if (ps.lc.fp32)
+			zeta_item<float>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+		else
+			zeta_item<double>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
 		if (tid == 0)
 		{
 			ps.lc.tile_total[r] = tile_total;
-			ps.lc.tile_scale[r] = tile_scale;
+			ps.lc.tile_scale[r] = scale;
 		}
 		done++;
 		// Count this CTA's finished items of the lattice when it moves on to
@@ -906,19 +1040,19 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 		if (wn >= total || wn >= lat_end)
 		{
 			LatticeDev &L = wm_state(states, wm, li);
-			__syncthreads();
+			zsync();
 			if (tid == 0)
 			{
-				if (ps.flag)
+				if (lat_bad)
 					atomicExch(&L.error, kErrNonFinite);
-				ps.flag = 0;
+				lat_bad = false;
 				bulk_wait_all(); // this lattice's q' stores are complete
 				__threadfence();
 				ps.last = atomicAdd(&L.k1_count, static_cast<unsigned int>(done)) ==
 						  items - static_cast<unsigned int>(done);
 			}
 			done = 0;
-			__syncthreads();
+			zsync();
 			if (ps.last)
 			{
 				__threadfence();
@@ -926,6 +1060,38 @@ __global__ void __launch_bounds__(kThreads, 1) k1_zeta_low(LatticeDev *states, W
 			}
 		}
 	}
+	if (tid == 0)
+		bulk_wait_all();
+}
+
+// K1: [update] -> per-tile fixed point -> zeta over the low t bits -> M1.
+// Grid: persistent, at most one CTA per work item; an item is one tile.
+// The update warps run the FP64 multiplies one tile ahead of the zeta
+// threads' integer and shared-memory work, so the two overlap.
+__global__ void __launch_bounds__(kK1Threads, 1) k1_zeta_low(LatticeDev *states, WorkMap wm)
+{
+	griddep_wait();
+	const ItemRange ir = item_range(wm);
+	if (ir.w >= ir.total)
+		return;
+	if (threadIdx.x == 0)
+	{
+		for (int i = 0; i < 2; i++)
+		{
+			mbar_init(&ps.bars[i], 1);
+			mbar_init(&ps.upd[i], 1);
+			mbar_init(&ps.freed[i], 1);
+		}
+		mbar_init_fence();
+		ps.lc.li = -1;
+		ps.uc.li = -1;
+		ps.abort = 0;
+	}
+	__syncthreads();
+	if (threadIdx.x >= kThreads)
+		k1_update_role(states, wm, ir);
+	else
+		k1_zeta_role(states, wm, ir);
 }
 
 // ------------------------------------------------------------------ K2

@@ -58,6 +58,8 @@ constexpr int kMaxMidBits = 6;                // middle pass: 13 + 6 + 11 = 30 a
 constexpr int kMaxAtoms = 30;
 constexpr int kMaxClasses = 32;               // likelihood classes for k = 1 (popcount 0..n)
 constexpr int kMaxClassTable = 4096;          // mixed-radix likelihood classes for k >= 2
+constexpr int kK1UpdThreads = 256;             // K1: the update warps beside the kThreads zeta threads
+constexpr int kK1Threads = kThreads + kK1UpdThreads;
 constexpr int kSmemBuf = kTileElems * 8;      // one 64 KB tile buffer
 constexpr int kPipeSmem = 3 * kSmemBuf;       // two bulk-copy buffers + one work buffer
 constexpr int kK2CtasPerSm = 2;               // K2 runs two one-tile CTAs per SM

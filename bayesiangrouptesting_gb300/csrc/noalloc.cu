@@ -233,7 +233,7 @@ extern "C" int bgt_gpu_select_noalloc(const double *posterior, int subjects, int
 		LatticeDev *state = reinterpret_cast<LatticeDev *>(scratch);
 		const int sms = sm_count();
 		const int per1 = 1 << g.hbits;
-		k1_zeta_low<<<per1 < sms ? per1 : sms, kThreads, k1_smem_bytes(), s>>>(state, WorkMap{1, per1, nullptr, nullptr});
+		k1_zeta_low<<<per1 < sms ? per1 : sms, kK1Threads, k1_smem_bytes(), s>>>(state, WorkMap{1, per1, nullptr, nullptr});
 		cuda_check(cudaGetLastError(), "noalloc k1 launch");
 		k2_zeta_high_select<<<g.nblk < kK2CtasPerSm * sms ? g.nblk : kK2CtasPerSm * sms, kThreads, k2_smem_bytes(g.hbits), s>>>(
 			state, WorkMap{1, g.nblk, nullptr, nullptr});

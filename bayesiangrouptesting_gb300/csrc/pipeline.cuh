@@ -34,6 +34,31 @@ __device__ __forceinline__ void proxy_fence()
 	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// One arrival (release) on a barrier initialised with count 1.
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Named barrier `id` over `count` threads (a multiple of 32; id 0 is
+// __syncthreads): the threads of one warp-specialised role synchronise
+// without the others.
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t count)
+{
+	asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// The same, returning whether any participating thread passed true.
+__device__ __forceinline__ bool named_sync_or(uint32_t id, uint32_t count, bool pred)
+{
+	uint32_t out;
+	asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+				 : "=r"(out)
+				 : "r"(static_cast<uint32_t>(pred)), "r"(id), "r"(count)
+				 : "memory");
+	return out != 0;
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
 {
 	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
