@@ -26,6 +26,7 @@ namespace bgt_gpu
 {
 
 __global__ void k1_zeta_low(LatticeDev *states, WorkMap wm);
+__global__ void wait_selftest(uint64_t limit_ns, int *out);
 __global__ void k2_zeta_high_select(LatticeDev *states, WorkMap wm);
 __global__ void kmid_zeta(LatticeDev *states, WorkMap wm);
 __global__ void posterior_diff_kernel(const LatticeDev *a, const LatticeDev *b, unsigned long long states,
@@ -531,6 +532,32 @@ const char *bgt_gpu_last_error(void) { return g_last_error.c_str(); }
 uint64_t bgt_gpu_kernel_launch_count(void) { return g_launches.load(); }
 
 int bgt_cuda_provider_available(void) { return device_present() ? 1 : 0; }
+
+int bgt_gpu_selftest_bounded_wait(uint32_t limit_us, int *timed_out)
+{
+	return guarded([&]() -> int {
+		if (!timed_out || limit_us == 0 || limit_us > 5000000u)
+		{
+			set_error("limit_us must be in 1 .. 5000000 and timed_out non-null");
+			return BGT_GPU_UNSUPPORTED;
+		}
+		int *d = nullptr;
+		cuda_check(cudaMalloc(&d, sizeof(int)), "self-test flag");
+		struct Free
+		{
+			int *p;
+			~Free() { cudaFree(p); }
+		} guard{d};
+		cuda_check(cudaMemset(d, 0xFF, sizeof(int)), "self-test flag init");
+		wait_selftest<<<1, 128>>>(static_cast<uint64_t>(limit_us) * 1000ull, d);
+		cuda_check(cudaGetLastError(), "self-test launch");
+		count_launches(1);
+		int h = -1;
+		cuda_check(cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost), "self-test result");
+		*timed_out = h;
+		return BGT_GPU_OK;
+	});
+}
 
 int bgt_gpu_profile_enable(int enable)
 {

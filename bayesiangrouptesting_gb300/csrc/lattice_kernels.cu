@@ -1094,6 +1094,25 @@ __global__ void __launch_bounds__(kK1Threads, 1) k1_zeta_low(LatticeDev *states,
 		k1_zeta_role(states, wm, ir);
 }
 
+// Self-test of the bounded waits every pass relies on: a barrier that
+// nothing arrives on, waited for by every thread with a limit of limit_ns.
+// out[0] = 1 when every wait gave up and the kernel returned (the context
+// stays usable), 0 if any wait saw the phase complete.
+__global__ void wait_selftest(uint64_t limit_ns, int *out)
+{
+	__shared__ uint64_t bar;
+	if (threadIdx.x == 0)
+	{
+		mbar_init(&bar, 1);
+		mbar_init_fence();
+	}
+	__syncthreads();
+	const bool completed = mbar_wait_bounded(&bar, 0u, limit_ns);
+	const int any = __syncthreads_or(completed);
+	if (threadIdx.x == 0)
+		out[0] = any ? 0 : 1;
+}
+
 // ------------------------------------------------------------------ K2
 
 typedef unsigned __int128 u128;

@@ -146,12 +146,13 @@ __device__ __forceinline__ uint64_t global_ns()
 	return t;
 }
 
-// Waits for phase `parity` of `bar` for at most ~2 s; false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+// Waits for phase `parity` of `bar` for at most limit_ns (default ~2 s);
+// false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns = 2000000000ull)
 {
 	if (mbar_try_wait(bar, parity))
 		return true;
-	const uint64_t deadline = global_ns() + 2000000000ull;
+	const uint64_t deadline = global_ns() + limit_ns;
 	for (uint32_t it = 0; it < (1u << 30); ++it)
 	{
 		if (mbar_try_wait(bar, parity))

@@ -218,6 +218,14 @@ BGT_GPU_API int bgt_gpu_profile_read(uint64_t *launches, double *milliseconds);
 BGT_GPU_API int bgt_gpu_select_noalloc(const double *posterior, int subjects, int selector, uint32_t *experiment,
 									   void *stream);
 
+/* Self-test of the bounded waits the kernels use on their bulk copies and
+ * hand-overs: one kernel waits, in 128 threads, on a shared-memory barrier
+ * that nothing completes, each wait limited to limit_us microseconds
+ * (1 .. 5000000).  *timed_out = 1 when every wait gave up and the kernel
+ * returned; the device stays usable afterwards.  No counterpart in the
+ * reference (its kernels do not wait on barriers). */
+BGT_GPU_API int bgt_gpu_selftest_bounded_wait(uint32_t limit_us, int *timed_out);
+
 /* Thread-local description of the last failure ("" when none). */
 BGT_GPU_API const char *bgt_gpu_last_error(void);
 

@@ -101,3 +101,19 @@ def test_selection_above_24_atoms_closed_form(gpu, oracle, n):
         assert abs(lat.upset_probability_mass(bgt.reverse_bits(e, n)) - mass(e)) <= 1e-12
     want = np.array([mass(1 << j) for j in range(n)])
     np.testing.assert_allclose(lat.atom_masses(), want, rtol=0, atol=1e-12)
+
+
+def test_bounded_wait_gives_up_and_device_stays_usable(gpu):
+    # Every kernel wait on a bulk copy or hand-over is bounded; a barrier that
+    # nothing completes must make the waits give up and the kernel return.
+    import ctypes
+    import time
+    from bayesiangrouptesting_gb300 import _native
+    lib = _native.load()
+    flag = ctypes.c_int(-1)
+    t0 = time.perf_counter()
+    assert lib.bgt_gpu_selftest_bounded_wait(20000, ctypes.byref(flag)) == 0
+    assert flag.value == 1
+    assert time.perf_counter() - t0 < 5.0
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 6, np.full(6, 0.1))
+    assert 0 <= lat.select_experiment() < 64  # the context still runs kernels
