@@ -11,15 +11,26 @@ from .api import (  # noqa: F401
     Lattice,
     LatticeType,
     Precision,
+    ProgressConfig,
     Provider,
+    ReportConfig,
     SelectorType,
     SimulationConfig,
+    SimulationMode,
     SimulationOptions,
     SimulationResult,
+    SimulationRunStatus,
+    SimulationTimings,
     StatusCode,
+    TerminationReason,
     TreeStats,
+    TrueStatePolicy,
     available_providers,
+    clear_simulation_cancellation,
     cuda_available,
+    request_simulation_cancellation,
+    simulation_cancellation_reason,
+    simulation_cancellation_requested,
     reverse_bits,
     run_simulation,
     select_experiment,

@@ -11,6 +11,8 @@ from __future__ import annotations
 
 import ctypes
 import enum
+import threading
+import time
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
@@ -190,26 +192,143 @@ class DilutionParameters:
     h: float = 0.005
 
 
+class SimulationMode(enum.IntEnum):
+    """bgt::SimulationMode (include/bgt/simulation.hpp:13-21).  Only
+    local_tree is served here; the parallel modes need the MPI backend."""
+
+    local_tree = 0
+    parallel_global_tree = 1
+    parallel_dynamic_tree = 2
+    parallel_hybrid_tree = 3
+    parallel_partial_tree = 4
+    parallel_fusion_tree = 5
+
+
+class TrueStatePolicy(enum.IntEnum):
+    """bgt::TrueStatePolicy (include/bgt/simulation.hpp:23-28)."""
+
+    all = 0
+    trimmed = 1
+    symmetric = 2
+
+
+class SimulationRunStatus(enum.IntEnum):
+    """bgt::SimulationRunStatus (include/bgt/simulation.hpp:30-35)."""
+
+    completed = 0
+    interrupted = 1
+    running = 2
+
+
+class TerminationReason(enum.IntEnum):
+    """bgt::TerminationReason (include/bgt/simulation.hpp:37-42)."""
+
+    none = 0
+    user_signal = 1
+    cancellation_requested = 2
+
+
+@dataclass
+class ReportConfig:
+    """bgt::ReportConfig (include/bgt/simulation.hpp:50-55)."""
+
+    write_csv: bool = False
+    output_directory: str = "."
+    run_name: str = ""
+
+
+@dataclass
+class ProgressConfig:
+    """bgt::ProgressConfig (include/bgt/simulation.hpp:65-72)."""
+
+    enabled: bool = False
+    interval_seconds: float = 5.0
+    output_path: str = ""
+    write_jsonl: bool = True
+    print_stderr: bool = False
+
+
+@dataclass
+class SimulationTimings:
+    """bgt::SimulationTimings (include/bgt/simulation.hpp:57-63)."""
+
+    setup_seconds: float = 0.0
+    tree_build_seconds: float = 0.0
+    evaluation_seconds: float = 0.0
+    total_seconds: float = 0.0
+
+
 @dataclass
 class SimulationConfig:
-    """The local_tree subset of bgt::SimulationConfig (include/bgt/simulation.hpp:87-103)."""
+    """bgt::SimulationConfig (include/bgt/simulation.hpp:87-103).  As on the
+    reference's CUDA path, evaluation_prior, true_state_policy, trim_percent,
+    global_tree_depth and workload_granularity do not change a local_tree run
+    on the device (every true state is evaluated under the prior)."""
 
     lattice_type: LatticeType = LatticeType.replicated_non_dilution
     subjects: int = 0
     variants: int = 1
     prior: Sequence[float] = field(default_factory=list)
+    evaluation_prior: Optional[Sequence[float]] = None
     options: SimulationOptions = field(default_factory=SimulationOptions)
+    mode: SimulationMode = SimulationMode.local_tree
+    true_state_policy: TrueStatePolicy = TrueStatePolicy.all
+    global_tree_depth: int = 0
+    workload_granularity: int = 1
+    trim_percent: float = 1.0
     dilution: DilutionParameters = field(default_factory=DilutionParameters)
+    report: ReportConfig = field(default_factory=ReportConfig)
+    progress: ProgressConfig = field(default_factory=ProgressConfig)
 
 
 @dataclass
 class SimulationResult:
-    """The local_tree subset of bgt::SimulationResult (include/bgt/simulation.hpp:105-121)."""
+    """bgt::SimulationResult (include/bgt/simulation.hpp:105-121), without the
+    KernelSpec."""
 
     stats: TreeStats
     provider: Provider
     total_states: int
     evaluated_states: int
+    mode: SimulationMode = SimulationMode.local_tree
+    rank: int = 0
+    world_size: int = 1
+    report_path: str = ""
+    timings: SimulationTimings = field(default_factory=SimulationTimings)
+    status: SimulationRunStatus = SimulationRunStatus.completed
+    termination_reason: TerminationReason = TerminationReason.none
+    evaluated_prior_mass: float = 0.0
+    progress_path: str = ""
+
+
+_cancel_lock = threading.Lock()
+_cancel_reason = TerminationReason.none
+
+
+def clear_simulation_cancellation() -> None:
+    """bgt::clear_simulation_cancellation (src/runtime/progress.cpp:84-87)."""
+    global _cancel_reason
+    with _cancel_lock:
+        _cancel_reason = TerminationReason.none
+
+
+def request_simulation_cancellation(reason: TerminationReason = TerminationReason.cancellation_requested) -> None:
+    """bgt::request_simulation_cancellation (src/runtime/progress.cpp:89-95):
+    the first request wins."""
+    global _cancel_reason
+    if reason == TerminationReason.none:
+        reason = TerminationReason.cancellation_requested
+    with _cancel_lock:
+        if _cancel_reason == TerminationReason.none:
+            _cancel_reason = reason
+
+
+def simulation_cancellation_requested() -> bool:
+    return _cancel_reason != TerminationReason.none
+
+
+def simulation_cancellation_reason() -> TerminationReason:
+    return _cancel_reason
 
 
 def cuda_available() -> bool:
@@ -225,18 +344,28 @@ def available_providers():
 
 
 def _validate(config: SimulationConfig) -> None:
-    """validate_simulation_config, src/runtime/simulation_runner.cpp:30-68 (local_tree part)."""
+    """validate_simulation_config, src/runtime/simulation_runner.cpp:30-68."""
     o = config.options
     if config.subjects <= 0 or config.variants <= 0 or o.search_depth < 0:
         raise ValueError("invalid simulation dimensions.")
+    if config.workload_granularity <= 0:
+        raise ValueError("workload_granularity must be positive.")
+    if config.progress.interval_seconds <= 0.0:
+        raise ValueError("progress interval must be positive.")
     if len(config.prior) != config.subjects * config.variants:
         raise ValueError("prior length must equal subjects * variants.")
+    if config.evaluation_prior is not None and len(config.evaluation_prior) != config.subjects * config.variants:
+        raise ValueError("evaluation_prior length must equal subjects * variants.")
     if _resolve_selector(o.selector, config.variants) == SelectorType.op_bha and config.variants != 1:
         raise ValueError("Op-BHA tree selection is only supported for binary lattices.")
     if _uses_dilution(config.lattice_type) and (config.dilution.alpha <= 0.0 or config.dilution.h <= 0.0):
         raise ValueError("dilution parameters must be positive.")
-    if config.lattice_type in (LatticeType.distributed_non_dilution, LatticeType.distributed_dilution):
+    if config.mode == SimulationMode.local_tree and config.lattice_type in (LatticeType.distributed_non_dilution,
+                                                                             LatticeType.distributed_dilution):
         raise ValueError("local_tree requires a replicated lattice.")
+    if config.mode != SimulationMode.local_tree:
+        raise Error(StatusCode.unsupported, "parallel simulation modes need the MPI backend; "
+                    "the GB300 provider serves local_tree on one GPU.")
 
 
 def run_simulation(config: SimulationConfig) -> SimulationResult:
@@ -245,12 +374,28 @@ def run_simulation(config: SimulationConfig) -> SimulationResult:
     CudaProvider::run, src/runtime/providers.cpp:73-133).  Provider.cpu is the
     reference library's own provider and is not served here; Provider.cuda
     and auto_select run on the device or raise."""
+    from .reporting import ProgressTracker, write_report_if_requested
+
+    total_start = time.perf_counter()
     _validate(config)
     if config.options.provider == Provider.cpu:
         raise Error(StatusCode.unsupported, "the CPU provider is the reference library's; this package is the CUDA provider")
+    total = 1 << (config.subjects * config.variants)
+    result = SimulationResult(TreeStats(), Provider.auto_select, total, 0, mode=config.mode)
+    progress = ProgressTracker(config, result.rank, result.total_states, total_start)
+    eval_start = time.perf_counter()
+    if simulation_cancellation_requested():
+        result.status = SimulationRunStatus.interrupted
+        result.termination_reason = simulation_cancellation_reason()
+        result.progress_path = progress.progress_path
+        result.timings.total_seconds = time.perf_counter() - total_start
+        progress.finish(result.status, result.termination_reason, "cancelled before evaluation started")
+        result.report_path = write_report_if_requested(config, result)
+        return result
     lib = load()
     if not lib.bgt_cuda_provider_available():
         raise Error(StatusCode.cuda_error, "CUDA provider requested, but no CUDA device is available.")
+    progress.maybe_emit("starting CUDA evaluation", force=True)
     prior = np.ascontiguousarray(config.prior, dtype=np.float64)
     dil = None
     if _uses_dilution(config.lattice_type):
@@ -262,8 +407,17 @@ def run_simulation(config: SimulationConfig) -> SimulationResult:
                                        int(_resolve_selector(config.options.selector, config.variants)),
                                        dil.rows() if dil else None, ctypes.byref(stats))
     _call(status)
-    total = 1 << (config.subjects * config.variants)
-    return SimulationResult(TreeStats.from_c(stats), Provider.cuda, total, total)
+    result.stats = TreeStats.from_c(stats)
+    result.provider = Provider.cuda
+    result.evaluated_states = total
+    result.evaluated_prior_mass = 1.0
+    progress.replace_state(result.evaluated_states, result.evaluated_prior_mass, result.stats)
+    result.timings.evaluation_seconds = time.perf_counter() - eval_start
+    result.timings.total_seconds = time.perf_counter() - total_start
+    result.progress_path = progress.progress_path
+    progress.finish(result.status, result.termination_reason, "completed")
+    result.report_path = write_report_if_requested(config, result)
+    return result
 
 
 class Lattice:
