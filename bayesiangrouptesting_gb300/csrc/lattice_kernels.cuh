@@ -19,7 +19,9 @@
 //
 // Stage structure for one binary (k = 1) lattice of n subjects, N = 2^n:
 //   K1 zeta_low   tiles of 2^t states (t = min(n, 13)), persistent CTAs fed
-//                 by bulk (TMA) copies double-buffered on mbarriers:
+//                 by bulk (TMA) copies double-buffered on mbarriers, each CTA
+//                 split into update warps (the FP64 multiplies, one tile
+//                 ahead) and zeta warps (everything else):
 //                 [apply pending update q *= L/Z] -> q (FP64, written back)
 //                 -> u64 at a per-tile scale -> zeta over the t low bits
 //                 -> partial sums M1 stored column-block-major (W columns
@@ -49,7 +51,7 @@ namespace bgt_gpu
 
 constexpr int kTileBits = 13;                 // states per K1 tile = 2^13 (64 KB of FP64)
 constexpr int kTileElems = 1 << kTileBits;
-constexpr int kThreads = 512;                 // both passes: 512 threads x 16 values
+constexpr int kThreads = 512;                 // both passes: 512 zeta threads x 16 values
 constexpr int kPerThread = kTileElems / kThreads;
 constexpr int kMaxColW = 16;                  // K2 block columns (u64 values per M1 row chunk)
 constexpr int kMinColW = 4;                   // 32-byte row chunks at the least
