@@ -755,14 +755,15 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 		fill_lattice_cache(L, li, ps.lc, threadIdx.x, true);
 }
 
-// The per-item constants from a lattice cache.
-__device__ __forceinline__ ItemCfg item_cfg(const LatCache &c, unsigned int r)
+// The per-lattice constants of an item from a lattice cache (phi, the
+// generated prior's row factor, is set by the caller that needs it).
+__device__ __forceinline__ ItemCfg item_cfg(const LatCache &c)
 {
 	ItemCfg cfg;
 	cfg.q_out = c.q_out;
 	cfg.m1 = c.m1;
 	cfg.prior_lo = c.prior_lo;
-	cfg.phi = c.mode == kGenerate ? c.prior_hi[r] : 0.0;
+	cfg.phi = 0.0;
 	cfg.e = c.e;
 	cfg.tbits = c.tbits;
 	cfg.hbits = c.hbits;
@@ -860,7 +861,9 @@ __device__ void k1_update_role(LatticeDev *states, const WorkMap &wm, ItemRange 
 			}
 			return;
 		}
-		const ItemCfg cfg = item_cfg(ps.uc, r);
+		ItemCfg cfg = item_cfg(ps.uc);
+		if (mode == kGenerate)
+			cfg.phi = ps.uc.prior_hi[r];
 		const unsigned int tsize = 1u << cfg.tbits;
 		const size_t base = static_cast<size_t>(r) << cfg.tbits;
 		float f = 0.0f;
@@ -1022,7 +1025,7 @@ __device__ void k1_zeta_role(LatticeDev *states, const WorkMap &wm, ItemRange ir
 		const int scale = ps.uscale[x];
 		if (tid == 0 && ps.ubad[x])
 			lat_bad = true;
-		ItemCfg cfg = item_cfg(ps.lc, r);
+		const ItemCfg cfg = item_cfg(ps.lc);
 		u64 tile_total = 0;
 		if (ps.lc.fp32)
 			zeta_item<float>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);

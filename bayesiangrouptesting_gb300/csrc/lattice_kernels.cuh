@@ -291,30 +291,39 @@ __device__ __forceinline__ unsigned long long to_fixed(double v, int scale)
 	return (m + (1ull << (rs - 1))) >> rs;
 }
 
-// round-half-up(v * 2^scale) for finite v >= 0 with v * 2^scale < 2^63,
-// branch-free.  With m the 53-bit significand, v * 2^scale =
-// (m << 11) / 2^rs for rs = 1086 - exponent - scale >= 1; rs is clamped to
-// 64, where the result is already 0 or 1 unit.
+// Shift right by rs bits with PTX semantics: an amount of 64 or more gives 0.
+__device__ __forceinline__ unsigned long long shr64(unsigned long long x, unsigned int rs)
+{
+	unsigned long long r;
+	asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(rs));
+	return r;
+}
+
+// floor(v * 2^scale) for finite v >= 0 with v * 2^scale < 2^63, branch-free:
+// with m the 53-bit significand, v * 2^scale = (m << 11) / 2^rs for
+// rs = 1086 - exponent - scale, which the per-tile scale keeps >= 1.
+// Truncation (error below one unit, never above the true value) rather than
+// rounding: every sum on the path is a sum of these same integers, so the
+// choice changes no comparison between them, and it saves the rounding add
+// and shift on the zeta threads' critical path.
 __device__ __forceinline__ unsigned long long to_fixed_fast(double v, int scale)
 {
 	const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
 	const int e = static_cast<int>(b >> 52);
 	const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (static_cast<unsigned long long>(e != 0) << 52);
-	int rs = 1086 - scale - (e > 1 ? e : 1);
-	rs = rs < 1 ? 1 : (rs > 64 ? 64 : rs);
-	return (((m << 11) >> (rs - 1)) + 1ull) >> 1;
+	const int rs = 1086 - scale - (e > 1 ? e : 1);
+	return shr64(m << 11, static_cast<unsigned int>(rs < 0 ? 0 : rs));
 }
 
-// The same rounding for an FP32 value (24-bit significand placed at bit 63):
+// The same for an FP32 value (24-bit significand placed at bit 63):
 // identical to to_fixed_fast of the value widened to FP64.
 __device__ __forceinline__ unsigned long long to_fixed_fast(float v, int scale)
 {
 	const unsigned int b = static_cast<unsigned int>(__float_as_int(v));
 	const int e = static_cast<int>(b >> 23);
 	const unsigned long long m = static_cast<unsigned long long>((b & 0x7FFFFFu) | (static_cast<unsigned int>(e != 0) << 23));
-	int rs = 190 - scale - (e > 1 ? e : 1);
-	rs = rs < 1 ? 1 : (rs > 64 ? 64 : rs);
-	return (((m << 40) >> (rs - 1)) + 1ull) >> 1;
+	const int rs = 190 - scale - (e > 1 ? e : 1);
+	return shr64(m << 40, static_cast<unsigned int>(rs < 0 ? 0 : rs));
 }
 
 // Non-finite (or, for the exponent test, huge) values trip the lattice's
