@@ -210,9 +210,6 @@ struct PipeShared
 extern __shared__ __align__(1024) unsigned char g_smem[];
 __shared__ PipeShared ps;
 __shared__ int g_shift[1 << kMaxHighBits];
-// The matching rounding offsets 2^(shift - 1) (0 for shift 0): the rescale
-// round-half-up(v / 2^s) is (v + half) >> s.
-__shared__ u64 g_half[1 << kMaxHighBits];
 // Mixed-radix likelihood classes of a multinomial update: entry
 // sum_v c_v * radix^v holds prod_v f_v(c_v) / Z (variant order, as
 // response_prob multiplies them, src/core/model/replicated_lattice.cpp:8-28).
@@ -320,7 +317,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 	const int s_g = min(1084 - ez, smin);
 	u64 zg = 0;
 	for (unsigned int rr = tid; rr < rows; rr += kThreads)
-		zg += shr_round(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
+		zg += to_global(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
 	for (int o = 16; o > 0; o >>= 1)
 		zg += __shfl_xor_sync(0xFFFFFFFFu, zg, o);
 	zsync();
@@ -342,7 +339,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 				const unsigned int col = 1u << atom;
 				const u64 *src = L.m1 + (static_cast<size_t>(col >> logw) * rows) * L.colw + (col & (L.colw - 1));
 				for (unsigned int rr = lane; rr < rows; rr += 32)
-					acc += shr_round(__ldcg(src + static_cast<size_t>(rr) * L.colw),
+					acc += to_global(__ldcg(src + static_cast<size_t>(rr) * L.colw),
 									 min(__ldcg(L.tile_scale + rr) - s_g, 63));
 			}
 			else
@@ -350,7 +347,7 @@ __device__ void k1_epilogue(LatticeDev &L, int mode)
 				const unsigned int hb = 1u << (atom - tbits);
 				for (unsigned int rr = lane; rr < rows; rr += 32)
 					if (rr & hb)
-						acc += shr_round(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
+						acc += to_global(__ldcg(L.tile_total + rr), min(__ldcg(L.tile_scale + rr) - s_g, 63));
 			}
 			for (int o = 16; o > 0; o >>= 1)
 				acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
@@ -1324,7 +1321,6 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 	u64 *const tile = tile_u64(0);
 	u64 *const work = tile;
 	int *const shift = g_shift;
-	u64 *const half = g_half;
 	const unsigned int tid = threadIdx.x;
 	const unsigned int sa = swz_a_base(tid), sb = swz_b_base(tid), sc = swz_c_base(tid), sd = swz_d_base(tid);
 	(void)sa;
@@ -1417,7 +1413,6 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 			{
 				const int sh = Lc.mbits ? 0 : min(Lc.tile_scale[rr] - s_g, 63);
 				shift[rr] = sh;
-				half[rr] = sh ? (1ull << (sh - 1)) : 0ull;
 			}
 			__syncthreads();
 		}
@@ -1460,9 +1455,8 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 			{
 				p = *reinterpret_cast<const ulonglong2 *>(in + y);
 				const int rs = shift[y >> logw];
-				const u64 hf = half[y >> logw];
-				p.x = (p.x + hf) >> rs; // = shr_round(p.x, rs) for p.x < 2^63
-				p.y = (p.y + hf) >> rs;
+				p.x = to_global(p.x, rs);
+				p.y = to_global(p.y, rs);
 			}
 			a[2 * i] = p.x;
 			a[2 * i + 1] = p.y;
@@ -1720,8 +1714,8 @@ __global__ void __launch_bounds__(kThreads, 1) kmid_zeta(LatticeDev *states, Wor
 			const unsigned int y = map_a(tid, 2 * i);
 			ulonglong2 p = *reinterpret_cast<const ulonglong2 *>(in + y);
 			const int rs = min(__ldg(tile_scale + row0 + (y >> 2)) - s_g, 63);
-			a[2 * i] = shr_round(p.x, rs);
-			a[2 * i + 1] = shr_round(p.y, rs);
+			a[2 * i] = to_global(p.x, rs);
+			a[2 * i + 1] = to_global(p.y, rs);
 		}
 		levels_a(a, mask);
 #pragma unroll

@@ -14,8 +14,9 @@
 // 64-bit fixed point on the integer pipes.  Each element costs at most one
 // FP64 multiply (the likelihood factor).  Because integer addition is exact
 // and associative, the zeta levels may run in any order and any tiling and the
-// result is bit-identical run to run; the only rounding is the one conversion
-// of each input to fixed point.
+// result is bit-identical run to run; the only roundings are the conversion of
+// each input to fixed point at its tile's scale and one truncating shift of
+// each partial sum to the lattice's global scale.
 //
 // Stage structure for one binary (k = 1) lattice of n subjects, N = 2^n:
 //   K1 zeta_low   tiles of 2^t states (t = min(n, 13)), persistent CTAs fed
@@ -331,11 +332,11 @@ __device__ __forceinline__ unsigned long long to_fixed_fast(float v, int scale)
 __device__ __forceinline__ bool non_finite(double v) { return __double2hiint(v) >= 0x7FF00000; }
 __device__ __forceinline__ bool non_finite(float v) { return __float_as_int(v) >= 0x7F800000; }
 
-// round-half-up(v / 2^rs) for 0 <= rs <= 63 and v < 2^63, branch-free.
-__device__ __forceinline__ unsigned long long shr_round(unsigned long long v, int rs)
-{
-	return (((v << 1) >> rs) + 1ull) >> 1;
-}
+// A tile's fixed-point value at the lattice's global scale: floor(v / 2^rs)
+// for 0 <= rs <= 63.  Every pass rescales with this one function (the total
+// Z_g, the atom masses, the middle pass and the high-bit pass), so the sums
+// they compare are sums of the same integers.
+__device__ __forceinline__ unsigned long long to_global(unsigned long long v, int rs) { return v >> rs; }
 
 // round(v * 2^d) for a fixed-point value v.
 __device__ __forceinline__ unsigned long long rescale(unsigned long long v, int d)
