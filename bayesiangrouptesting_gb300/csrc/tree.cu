@@ -41,7 +41,7 @@ namespace bgt_gpu
 __global__ void prior_tables(const double *pi0, int atoms, int tbits, double *lo, double *hi);
 
 constexpr int kSweepThreads = 256;
-constexpr int kMaxTreeNodes = 4096; // preorder nodes held in shared memory
+constexpr int kMaxTreeNodes = 4096; // preorder nodes the sweep walks
 constexpr int kMaxDepth = 30;
 
 struct SweepNode
@@ -264,92 +264,144 @@ __global__ void tree_expand(const LatticeDev *parents, LatticeDev *children, con
 	child_nodes[c] = nd;
 }
 
+constexpr int kFlattenThreads = 1024;
+
 // Preorder list of the existing nodes (children in response order), with
-// each node's subtree end, and the sum of the leaves' contributions in the
-// same order; one thread.
-__global__ void tree_flatten(const TreeNodeRec *recs, const long long *level_off, int depth, int R, int atoms,
-							 SweepNode *out, int capacity, TreeFlatOut *res)
+// each node's subtree end, the leaf count, the first error in preorder and
+// the sum of the leaves' contributions; one CTA, level by level:
+//   sizes bottom-up:  size(s) = 1 + sum of the children's sizes (0 for a
+//                     missing slot; a leaf has no children),
+//   indices top-down: the first child sits right after its parent, each next
+//                     child after the previous child's subtree,
+// then every node writes its entry at its index.  The contributions are
+// summed over the slots in a fixed order (each thread a contiguous range,
+// the ranges in thread order), so the result is the same run to run.
+// `size` and `index` are scratch arrays of one int per slot.
+__global__ void __launch_bounds__(kFlattenThreads) tree_flatten(const TreeNodeRec *recs, const long long *level_off,
+																int depth, int R, int atoms, SweepNode *out, int capacity,
+																int *size, int *index, TreeFlatOut *res)
 {
-	if (threadIdx.x != 0 || blockIdx.x != 0)
-		return;
-	int stack_idx[kMaxDepth + 2];
-	long long stack_slot[kMaxDepth + 2];
-	int stack_r[kMaxDepth + 2];
-	int n = 0, leaves = 0, err = 0, top = 0;
+	const int tid = threadIdx.x;
+	__shared__ unsigned long long first_error;
+	__shared__ int leaves_sum;
+	__shared__ double part[kFlattenThreads / 32][7];
+	if (tid == 0)
+	{
+		first_error = ~0ull;
+		leaves_sum = 0;
+	}
+	// Sizes, deepest level first.
+	for (int d = depth; d >= 0; d--)
+	{
+		const long long off = level_off[d], count = level_off[d + 1] - off;
+		for (long long sl = tid; sl < count; sl += kFlattenThreads)
+		{
+			const TreeNodeRec &me = recs[off + sl];
+			int sz = 0;
+			if (me.exists)
+			{
+				sz = 1;
+				if (!me.leaf && d < depth)
+					for (int i = 0; i < R; i++)
+						sz += size[level_off[d + 1] + sl * R + i];
+			}
+			size[off + sl] = sz;
+		}
+		__syncthreads();
+	}
+	// Preorder indices, root first.
+	if (tid == 0)
+		index[0] = 0;
+	__syncthreads();
+	for (int d = 0; d < depth; d++)
+	{
+		const long long off = level_off[d], count = level_off[d + 1] - off;
+		for (long long sl = tid; sl < count; sl += kFlattenThreads)
+		{
+			const TreeNodeRec &me = recs[off + sl];
+			if (!me.exists || me.leaf)
+				continue;
+			int next = index[off + sl] + 1;
+			for (int i = 0; i < R; i++)
+			{
+				const long long c = level_off[d + 1] + sl * R + i;
+				index[c] = next;
+				next += size[c];
+			}
+		}
+		__syncthreads();
+	}
+	// Entries, leaves, first error, contributions.
+	const long long total = level_off[depth + 1];
+	const long long chunk = (total + kFlattenThreads - 1) / kFlattenThreads;
+	const long long lo = tid * chunk, hi = lo + chunk < total ? lo + chunk : total;
 	double st[7] = {0, 0, 0, 0, 0, 0, 0};
-	auto add_leaf = [&](const TreeNodeRec &r) {
-		if (!r.leaf)
-			return;
-		for (int j = 0; j < 5; j++)
-			st[j] += r.stat[j];
-		st[5] += r.stage * r.path;
-		st[6] += r.stage * r.path;
-	};
-	// Root.
-	stack_slot[0] = 0;
-	stack_r[0] = 0;
+	int leaves = 0;
+	int d = 0;
+	for (long long sl = lo; sl < hi; sl++)
 	{
-		const TreeNodeRec &rt = recs[0];
-		SweepNode sn{};
-		sn.ex = rt.ex;
-		sn.res = rt.res;
-		sn.pos = rt.pos;
-		sn.neg = rt.neg;
-		sn.stage = 0;
-		sn.leaf = rt.leaf;
-		sn.classified = __popc(rt.pos | rt.neg) == atoms ? 1 : 0;
-		out[0] = sn;
-		stack_idx[0] = 0;
-		n = 1;
-		leaves += rt.leaf;
-		add_leaf(rt);
-		err = rt.error;
-	}
-	while (top >= 0)
-	{
-		const int d = top;
-		const long long slot = stack_slot[top];
-		const TreeNodeRec &me = recs[level_off[d] + slot];
-		if (me.leaf || d >= depth || stack_r[top] >= R)
-		{
-			out[stack_idx[top]].end = n;
-			top--;
+		while (sl >= level_off[d + 1])
+			d++;
+		const TreeNodeRec &me = recs[sl];
+		if (!me.exists)
 			continue;
-		}
-		const long long cs = slot * R + stack_r[top];
-		stack_r[top]++;
-		const TreeNodeRec &ch = recs[level_off[d + 1] + cs];
-		if (!ch.exists)
-			continue;
-		if (n >= capacity)
+		const int at = index[sl];
+		if (me.error)
+			atomicMin(&first_error, (static_cast<unsigned long long>(at) << 32) | static_cast<unsigned int>(me.error));
+		if (at < capacity)
 		{
-			err = 1 << 20;
-			break;
+			SweepNode sn{};
+			sn.ex = d ? me.ex : 0u;
+			sn.res = d ? me.res : 0u;
+			sn.pos = me.pos;
+			sn.neg = me.neg;
+			sn.stage = d;
+			sn.leaf = me.leaf || d >= depth ? 1 : 0;
+			sn.classified = __popc(me.pos | me.neg) == atoms ? 1 : 0;
+			sn.end = at + size[sl];
+			out[at] = sn;
 		}
-		SweepNode sn{};
-		sn.ex = ch.ex;
-		sn.res = ch.res;
-		sn.pos = ch.pos;
-		sn.neg = ch.neg;
-		sn.stage = ch.stage;
-		sn.leaf = ch.leaf;
-		sn.classified = __popc(ch.pos | ch.neg) == atoms ? 1 : 0;
-		out[n] = sn;
-		leaves += ch.leaf;
-		add_leaf(ch);
-		if (!err)
-			err = ch.error;
-		top++;
-		stack_idx[top] = n;
-		stack_slot[top] = cs;
-		stack_r[top] = 0;
-		n++;
+		if (me.leaf)
+		{
+			leaves++;
+			for (int j = 0; j < 5; j++)
+				st[j] += me.stat[j];
+			st[5] += me.stage * me.path;
+			st[6] += me.stage * me.path;
+		}
 	}
-	res->count = n;
-	res->leaves = leaves;
-	res->error = err;
+	atomicAdd(&leaves_sum, leaves);
+	// Contributions: warps in thread order, then the warps in order.
 	for (int j = 0; j < 7; j++)
-		res->stats[j] = st[j];
+	{
+		double v = st[j];
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			const double w = __shfl_down_sync(0xFFFFFFFFu, v, o);
+			if ((tid & 31) % (2 * o) == 0)
+				v += w;
+		}
+		if ((tid & 31) == 0)
+			part[tid >> 5][j] = v;
+	}
+	__syncthreads();
+	if (tid == 0)
+	{
+		const int count = size[0];
+		int err = first_error == ~0ull ? 0 : static_cast<int>(first_error & 0xFFFFFFFFull);
+		if (count > capacity)
+			err = 1 << 20;
+		res->count = count < capacity ? count : capacity;
+		res->leaves = leaves_sum;
+		res->error = err;
+		for (int j = 0; j < 7; j++)
+		{
+			double v = 0.0;
+			for (int w = 0; w < kFlattenThreads / 32; w++)
+				v += part[w][j];
+			res->stats[j] = v;
+		}
+	}
 }
 
 namespace
@@ -486,6 +538,7 @@ struct TreeGraph
 	long long *level_off = nullptr;
 	SweepNode *flat = nullptr;
 	TreeFlatOut *flat_out = nullptr;
+	int *flat_size = nullptr, *flat_index = nullptr; // per-slot scratch of the flatten pass
 	double *partials = nullptr;
 	double *d_pi0 = nullptr, *d_dil = nullptr, *d_lo = nullptr, *d_hi = nullptr, *d_thres = nullptr;
 	unsigned int *blk_list = nullptr, *cblk_list = nullptr; // k >= 2: blocks BBPA reads
@@ -593,6 +646,8 @@ void build_tree_graph(TreeGraph &t)
 			   "level offsets up");
 	t.flat = t.dev<SweepNode>(kMaxTreeNodes, "alloc sweep nodes");
 	t.flat_out = t.dev<TreeFlatOut>(1, "alloc flatten result");
+	t.flat_size = t.dev<int>(static_cast<size_t>(t.total_nodes), "alloc flatten sizes");
+	t.flat_index = t.dev<int>(static_cast<size_t>(t.total_nodes), "alloc flatten indices");
 	t.d_pi0 = t.dev<double>(static_cast<size_t>(g.atoms), "alloc pi0");
 	t.d_dil = t.dev<double>(static_cast<size_t>(g.n) * (g.n + 1), "alloc dilution");
 	t.d_lo = t.dev<double>(size_t{1} << g.tbits, "alloc prior lo");
@@ -729,7 +784,8 @@ uint64_t enqueue_tree(TreeGraph &t)
 		off += count;
 		count = nchild;
 	}
-	tree_flatten<<<1, 32, 0, s>>>(t.recs, t.level_off, t.depth, t.R, g.atoms, t.flat, kMaxTreeNodes, t.flat_out);
+	tree_flatten<<<1, kFlattenThreads, 0, s>>>(t.recs, t.level_off, t.depth, t.R, g.atoms, t.flat, kMaxTreeNodes,
+											   t.flat_size, t.flat_index, t.flat_out);
 	cuda_check(cudaGetLastError(), "tree flatten");
 	count_launches(1);
 	kernels++;
