@@ -468,8 +468,79 @@ __device__ __forceinline__ int multinomial_class(const ItemCfg &cfg, unsigned in
 }
 
 // Likelihood-class kinds of an update: containment (non-dilution), popcount
-// of e & s (dilution), mixed radix over variants (k >= 2).
-constexpr int kClsContained = 0, kClsPopcount = 1, kClsMulti = 2;
+// of e & s (dilution), mixed radix over variants (k >= 2) in general, and
+// mixed radix through a per-tile plan with 1 .. 4 variants that vary inside
+// the tile (kClsPlan + that count).
+constexpr int kClsContained = 0, kClsPopcount = 1, kClsMulti = 2, kClsPlan = 3;
+constexpr int kMaxPlanVary = 4;
+
+// The mixed-radix class of the states of one tile, split into the part the
+// tile's base index fixes and the part that varies with the in-tile index x
+// (the two occupy disjoint bits).  Variant v's subjects are state bits
+// v n .. v n + n - 1; only variants with v n < tbits reach into x.
+//   containment: class bit c_v = [e subset of s_v] = [need_v subset of x_v],
+//                need_v = the bits of e the base does not supply;
+//   dilution:    c_v = popcount(e & s_v) = popcount(e & base_v) + popcount(e & x_v).
+// The fixed parts are summed into idx0; per element only the varying
+// variants are evaluated.
+struct ClassPlan
+{
+	int idx0;
+	int nvary;
+	unsigned int sh[kMaxPlanVary];   // v n
+	unsigned int mk[kMaxPlanVary];   // need_v (containment) or e (dilution)
+	int w[kMaxPlanVary];             // radix^v
+};
+
+__device__ __forceinline__ ClassPlan class_plan(const ItemCfg &cfg, size_t base)
+{
+	// The varying variants are the first ones: v = 0 .. nvary - 1.
+	ClassPlan p;
+	const unsigned int mask = (1u << cfg.n) - 1u;
+	const bool dil = cfg.dilution_classes != 0;
+	p.nvary = (cfg.tbits + cfg.n - 1) / cfg.n;
+	if (p.nvary > cfg.k)
+		p.nvary = cfg.k;
+	p.idx0 = 0;
+	int w = 1;
+#pragma unroll
+	for (int i = 0; i < kMaxPlanVary; i++)
+	{
+		const int shv = i * cfg.n;
+		const unsigned int bv = shv < 64 ? static_cast<unsigned int>(base >> shv) & mask : 0u;
+		p.sh[i] = static_cast<unsigned int>(shv < 31 ? shv : 31);
+		p.mk[i] = dil ? cfg.e : (cfg.e & ~bv);
+		p.w[i] = w;
+		if (i < p.nvary && dil)
+			p.idx0 += __popc(cfg.e & bv) * w;
+		w *= cfg.radix;
+	}
+	w = 1;
+	for (int v = 0; v < cfg.k; v++)
+	{
+		if (v >= p.nvary)
+		{
+			const unsigned int bv = static_cast<unsigned int>(base >> (v * cfg.n)) & mask;
+			p.idx0 += dil ? __popc(cfg.e & bv) * w : ((cfg.e & ~bv) == 0 ? w : 0);
+		}
+		w *= cfg.radix;
+	}
+	return p;
+}
+
+// The class of in-tile index x under a plan with kVary varying variants.
+template <int kVary>
+__device__ __forceinline__ int plan_class(const ClassPlan &p, bool dilution, unsigned int x)
+{
+	int idx = p.idx0;
+#pragma unroll
+	for (int i = 0; i < kVary; i++)
+	{
+		const unsigned int xv = (x >> p.sh[i]) & p.mk[i];
+		idx += dilution ? __popc(xv) * p.w[i] : (xv == p.mk[i] ? p.w[i] : 0);
+	}
+	return idx;
+}
 
 // The update warps' pass over one tile in shared buffer `in` (thread tu
 // takes elements tu + 128 k: a warp reads 32 consecutive values): generate
@@ -480,7 +551,7 @@ constexpr int kClsContained = 0, kClsPopcount = 1, kClsMulti = 2;
 // keep the FP64 pipe busy.
 template <int kMode, typename T, int kCls>
 __device__ __forceinline__ void update_tile(const ItemCfg &cfg, T *in, size_t base, unsigned int tsize,
-											unsigned int tu, float &f, bool &bad)
+											unsigned int tu, float &f, bool &bad, const ClassPlan &plan)
 {
 	constexpr int kBatch = 8;
 	const unsigned int e = cfg.e;
@@ -506,6 +577,8 @@ __device__ __forceinline__ void update_tile(const ItemCfg &cfg, T *in, size_t ba
 				const unsigned int s0 = static_cast<unsigned int>(base) | x;
 				if (kMode != kUpdate)
 					c[j] = T(1);
+				else if (kCls > kClsPlan)
+					c[j] = multinomial_factor<T>(plan_class<kCls - kClsPlan>(plan, cfg.dilution_classes != 0, x));
 				else if (kCls == kClsMulti)
 					c[j] = multinomial_factor<T>(multinomial_class(cfg, s0));
 				else if (kCls == kClsPopcount)
@@ -541,12 +614,34 @@ template <int kMode, typename T>
 __device__ __forceinline__ void update_tile_any(const ItemCfg &cfg, T *in, size_t base, unsigned int tsize,
 												unsigned int tu, float &f, bool &bad)
 {
+	ClassPlan plan;
+	plan.nvary = 0;
 	if (kMode == kUpdate && cfg.k > 1)
-		update_tile<kMode, T, kClsMulti>(cfg, in, base, tsize, tu, f, bad);
+	{
+		plan = class_plan(cfg, base);
+		switch (plan.nvary)
+		{
+		case 1:
+			update_tile<kMode, T, kClsPlan + 1>(cfg, in, base, tsize, tu, f, bad, plan);
+			break;
+		case 2:
+			update_tile<kMode, T, kClsPlan + 2>(cfg, in, base, tsize, tu, f, bad, plan);
+			break;
+		case 3:
+			update_tile<kMode, T, kClsPlan + 3>(cfg, in, base, tsize, tu, f, bad, plan);
+			break;
+		case 4:
+			update_tile<kMode, T, kClsPlan + 4>(cfg, in, base, tsize, tu, f, bad, plan);
+			break;
+		default:
+			update_tile<kMode, T, kClsMulti>(cfg, in, base, tsize, tu, f, bad, plan);
+			break;
+		}
+	}
 	else if (kMode == kUpdate && cfg.dilution_classes)
-		update_tile<kMode, T, kClsPopcount>(cfg, in, base, tsize, tu, f, bad);
+		update_tile<kMode, T, kClsPopcount>(cfg, in, base, tsize, tu, f, bad, plan);
 	else
-		update_tile<kMode, T, kClsContained>(cfg, in, base, tsize, tu, f, bad);
+		update_tile<kMode, T, kClsContained>(cfg, in, base, tsize, tu, f, bad, plan);
 }
 
 // Tile scale from the summed estimate: the tile total lands in

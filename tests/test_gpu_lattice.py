@@ -126,7 +126,9 @@ def test_multinomial_reference_pin(gpu, oracle):
 
 
 @pytest.mark.parametrize("k,n,dilution", [(2, 3, False), (2, 6, True), (2, 9, False), (2, 12, True), (3, 4, False),
-                                          (3, 6, True), (3, 8, False), (4, 5, False)])
+                                          (3, 6, True), (3, 8, False), (4, 5, False),
+                                          # five or more variants inside one tile: the general class path
+                                          (6, 3, False), (5, 3, True)])
 def test_multinomial_session_matches_oracle(gpu, oracle, k, n, dilution):
     rng = np.random.default_rng(1000 + 10 * k + n)
     pi0 = rng.uniform(0.01, 0.12, n * k)
