@@ -656,7 +656,7 @@ __device__ __forceinline__ int tile_scale_of(float est)
 // warps in buffer x, with scale `scale`): bulk-store q' (store_q), convert to
 // fixed point, release the buffer (issue2() then starts the copy of the item
 // after next into it), run the 13 zeta levels and store the partial sums.
-template <typename T, typename Issue2>
+template <typename T, bool kFull, typename Issue2>
 __device__ __forceinline__ void zeta_item(const ItemCfg &cfg, unsigned int r, int x, int scale, bool store_q,
 										  Issue2 &&issue2, u64 &total_out)
 {
@@ -668,9 +668,11 @@ __device__ __forceinline__ void zeta_item(const ItemCfg &cfg, unsigned int r, in
 	(void)sb;
 	(void)sc;
 	(void)sd;
-	const int tbits = cfg.tbits;
+	// Full tiles (every lattice of at least 13 atoms) get every level and no
+	// bounds test at compile time: no branches between the zeta levels.
+	const int tbits = kFull ? kTileBits : cfg.tbits;
 	const unsigned int tsize = 1u << tbits;
-	const bool full = tsize == kTileElems;
+	const bool full = kFull || tsize == kTileElems;
 	const size_t base = static_cast<size_t>(r) << tbits;
 	if (store_q && tid == 0)
 	{
@@ -1119,10 +1121,21 @@ __device__ void k1_zeta_role(LatticeDev *states, const WorkMap &wm, ItemRange ir
 			lat_bad = true;
 		const ItemCfg cfg = item_cfg(ps.lc);
 		u64 tile_total = 0;
+		const bool full = cfg.tbits == kTileBits;
 		if (ps.lc.fp32)
-			zeta_item<float>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+		{
+			if (full)
+				zeta_item<float, true>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+			else
+				zeta_item<float, false>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+		}
 		else
-			zeta_item<double>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+		{
+			if (full)
+				zeta_item<double, true>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+			else
+				zeta_item<double, false>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+		}
 		if (tid == 0)
 		{
 			ps.lc.tile_total[r] = tile_total;
