@@ -7,6 +7,8 @@
 // completes its last work item.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "lattice_kernels.cuh"
 #include "pipeline.cuh"
 
@@ -1536,9 +1538,9 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 			continue;
 		}
 		const unsigned int blk = ps.lc.blk_list ? __ldg(ps.lc.blk_list + bitem) : bitem;
-		const int tbits = ps.lc.tbits, logw = ps.lc.logw, mbits = ps.lc.mbits;
+		const int tbits = ps.lc.tbits, logw_rt = ps.lc.logw, mbits = ps.lc.mbits;
 		const unsigned int rows = 1u << (ps.lc.hbits - mbits);
-		const unsigned int elems = rows << logw;
+		const unsigned int elems_rt = rows << logw_rt;
 		// Block index: column block and, above 24 atoms, the middle index.
 		const unsigned int r_lo = blk & ((1u << mbits) - 1u);
 		const unsigned int cblk = blk >> mbits;
@@ -1547,145 +1549,167 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 		const unsigned int active = ps.lc.active;
 		const unsigned int all = ps.lc.n >= 32 ? 0xFFFFFFFFu : ((1u << ps.lc.n) - 1u);
 		const bool want_masses = ps.lc.masses != 0 && ((blk >> ps.lc.mbits) & ((blk >> ps.lc.mbits) - 1u)) == 0;
-		const bool timed_out = issued && !mbar_wait_bounded(&ps.bars[0], parity);
-		if (issued)
-			parity ^= 1u;
-		// Row bits of the block index y = row * W + column.
-		const unsigned int mask = (rows - 1u) << logw;
-		const u64 *in = tile;
-		u64 a[kPerThread];
+		// One item, specialised on the block geometry: kLogW = log2 W for full
+		// 8192-value blocks (row bits and bounds known at compile time, no
+		// branches between the zeta levels), 0 for the general case.
+		// Returns true when the item's copy timed out.
+		u64 best = ~0ull;
+		unsigned int best_e = 0xFFFFFFFFu;
+		auto item = [&](auto lw) -> bool {
+			constexpr int kLogW = decltype(lw)::value;
+			const int logw = kLogW ? kLogW : logw_rt;
+			const unsigned int elems = kLogW ? static_cast<unsigned int>(kTileElems) : elems_rt;
+			const bool timed_out = issued && !mbar_wait_bounded(&ps.bars[0], parity);
+			if (issued)
+				parity ^= 1u;
+			// Row bits of the block index y = row * W + column.
+			const unsigned int mask = kLogW ? ((kTileElems - 1u) & ~((1u << kLogW) - 1u)) : (rows - 1u) << logw;
+			const u64 *in = tile;
+			u64 a[kPerThread];
 #pragma unroll
-		for (int i = 0; i < kPerThread / 2; i++)
-		{
-			const unsigned int y = map_a(tid, 2 * i);
-			ulonglong2 p = make_ulonglong2(0ull, 0ull);
-			if (y < elems)
+			for (int i = 0; i < kPerThread / 2; i++)
 			{
-				p = *reinterpret_cast<const ulonglong2 *>(in + y);
-				const int rs = shift[y >> logw];
-				p.x = to_global(p.x, rs);
-				p.y = to_global(p.y, rs);
+				const unsigned int y = map_a(tid, 2 * i);
+				ulonglong2 p = make_ulonglong2(0ull, 0ull);
+				if (kLogW || y < elems)
+				{
+					p = *reinterpret_cast<const ulonglong2 *>(in + y);
+					const int rs = shift[y >> logw];
+					p.x = to_global(p.x, rs);
+					p.y = to_global(p.y, rs);
+				}
+				a[2 * i] = p.x;
+				a[2 * i + 1] = p.y;
 			}
-			a[2 * i] = p.x;
-			a[2 * i + 1] = p.y;
-		}
-		levels_a(a, mask);
-		// Every thread has read its values from the tile: it becomes the work tile.
-		if (__syncthreads_or(timed_out))
-		{
+			levels_a(a, mask);
+			// Every thread has read its values from the tile: it becomes the work tile.
+			if (__syncthreads_or(timed_out))
+			{
+				if (tid == 0)
+				{
+					atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
+					mbar_wait_bounded(&ps.bars[0], parity ^ 1u); // the late copy still targets the tile
+				}
+				return true;
+			}
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+				work[swz_a(sa, j)] = a[j];
+			__syncthreads();
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+				a[j] = work[swz_b(sb, j)];
+			levels_b(a, mask);
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+				work[swz_b(sb, j)] = a[j];
+			__syncthreads();
+#pragma unroll
+			for (int j = 0; j < kPerThread; j++)
+				a[j] = work[swz_c(sc, j)];
+			// The tile is free: copy the next block while this one is scored.
+			__syncthreads();
 			if (tid == 0)
 			{
-				atomicExch(&wm_state(states, wm, li).error, kErrTimeout);
-				mbar_wait_bounded(&ps.bars[0], parity ^ 1u); // the late copy still targets the tile
+				proxy_fence();
+				ps.flag = (wn < total && issue(wn)) ? 1 : 0;
 			}
-			return;
-		}
-#pragma unroll
-		for (int j = 0; j < kPerThread; j++)
-			work[swz_a(sa, j)] = a[j];
-		__syncthreads();
-#pragma unroll
-		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[swz_b(sb, j)];
-		levels_b(a, mask);
-#pragma unroll
-		for (int j = 0; j < kPerThread; j++)
-			work[swz_b(sb, j)] = a[j];
-		__syncthreads();
-#pragma unroll
-		for (int j = 0; j < kPerThread; j++)
-			a[j] = work[swz_c(sc, j)];
-		// The tile is free: copy the next block while this one is scored.
-		__syncthreads();
-		if (tid == 0)
-		{
-			proxy_fence();
-			ps.flag = (wn < total && issue(wn)) ? 1 : 0;
-		}
-		levels_c(a, mask);
-		// All row bits are done (W >= 4, so y bits 0..1 are column bits).
-		// Score |2 M(E) - Z_g|; within a thread E grows with j, so a strict
-		// comparison keeps the lowest index on ties.
-		const unsigned int col_base = (r_lo << tbits) | (cblk << logw);
-		const unsigned int wmask = (1u << logw) - 1u;
-		const unsigned int y0 = map_c(tid, 0);
-		u64 best = ~0ull;
-		int best_j = -1;
-		if (ps.lc.k > 1)
-		{
-			// Multinomial: keep the zeta values at the points sum_{v in B} E << (v n),
-			// which are the BBPA feature masses F_B(E) (bbpa.cpp:222-285); the
-			// lattice's last block scores them.
-			const int nn = ps.lc.n, kk = ps.lc.k;
-			const unsigned int nmask = (1u << nn) - 1u;
-			u64 *ftab = ps.lc.ftab;
-#pragma unroll
-			for (int j = 0; j < kPerThread; j++)
+			levels_c(a, mask);
+			// All row bits are done (W >= 4, so y bits 0..1 are column bits).
+			// Score |2 M(E) - Z_g|; within a thread E grows with j, so a strict
+			// comparison keeps the lowest index on ties.
+			const unsigned int col_base = (r_lo << tbits) | (cblk << logw);
+			const unsigned int wmask = (1u << logw) - 1u;
+			const unsigned int y0 = map_c(tid, 0);
+			int best_j = -1;
+			if (ps.lc.k > 1)
 			{
-				const unsigned int y = y0 + (j << 2);
-				if (y >= elems)
-					continue;
-				const unsigned int Eall = ((y >> logw) << row_shift) | col_base | (y & wmask);
-				unsigned int ev = 0, bset = 0;
-				bool diag = true;
-				for (int v = 0; v < kk; v++)
+				// Multinomial: keep the zeta values at the points sum_{v in B} E << (v n),
+				// which are the BBPA feature masses F_B(E) (bbpa.cpp:222-285); the
+				// lattice's last block scores them.
+				const int nn = ps.lc.n, kk = ps.lc.k;
+				const unsigned int nmask = (1u << nn) - 1u;
+				u64 *ftab = ps.lc.ftab;
+#pragma unroll
+				for (int j = 0; j < kPerThread; j++)
 				{
-					const unsigned int c = (Eall >> (v * nn)) & nmask;
-					if (c)
+					const unsigned int y = y0 + (j << 2);
+					if (y >= elems)
+						continue;
+					const unsigned int Eall = ((y >> logw) << row_shift) | col_base | (y & wmask);
+					unsigned int ev = 0, bset = 0;
+					bool diag = true;
+					for (int v = 0; v < kk; v++)
 					{
-						diag &= ev == 0 || c == ev;
-						ev = c;
-						bset |= 1u << v;
+						const unsigned int c = (Eall >> (v * nn)) & nmask;
+						if (c)
+						{
+							diag &= ev == 0 || c == ev;
+							ev = c;
+							bset |= 1u << v;
+						}
 					}
+					if (diag && bset)
+						ftab[(static_cast<size_t>(bset) << nn) | ev] = a[j];
 				}
-				if (diag && bset)
-					ftab[(static_cast<size_t>(bset) << nn) | ev] = a[j];
 			}
-		}
-		else if ((active & all) == all)
-		{
-#pragma unroll
-			for (int j = 0; j < kPerThread; j++)
+			else if ((active & all) == all)
 			{
-				const u64 score = abs_score(a[j], zg);
-				const bool take = (y0 + (j << 2)) < elems && score < best;
-				best = take ? score : best;
-				best_j = take ? j : best_j;
+#pragma unroll
+				for (int j = 0; j < kPerThread; j++)
+				{
+					const u64 score = abs_score(a[j], zg);
+					const bool take = (kLogW || (y0 + (j << 2)) < elems) && score < best;
+					best = take ? score : best;
+					best_j = take ? j : best_j;
+				}
 			}
-		}
+			else
+			{
+#pragma unroll
+				for (int j = 0; j < kPerThread; j++)
+				{
+					const unsigned int y = y0 + (j << 2);
+					const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
+					const u64 score = abs_score(a[j], zg);
+					const bool take = y < elems && (E & ~active) == 0 && score < best;
+					best = take ? score : best;
+					best_j = take ? j : best_j;
+				}
+			}
+			if (best_j >= 0)
+			{
+				const unsigned int y = y0 + (best_j << 2);
+				best_e = ((y >> logw) << row_shift) | col_base | (y & wmask);
+			}
+			LatticeDev &L = wm_state(states, wm, li);
+			// Singleton (atom) masses live in block 0 and in the blocks whose
+			// first column is a power of two.
+			if (want_masses)
+			{
+#pragma unroll
+				for (int j = 0; j < kPerThread; j++)
+				{
+					const unsigned int y = y0 + (j << 2);
+					const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
+					if (y < elems && __popc(E) == 1)
+						L.atom_fixed[__ffs(E) - 1] = a[j];
+				}
+			}
+			return false;
+		};
+		bool aborted;
+		if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 2)
+			aborted = item(std::integral_constant<int, 2>{});
+		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 3)
+			aborted = item(std::integral_constant<int, 3>{});
+		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 4)
+			aborted = item(std::integral_constant<int, 4>{});
 		else
-		{
-#pragma unroll
-			for (int j = 0; j < kPerThread; j++)
-			{
-				const unsigned int y = y0 + (j << 2);
-				const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
-				const u64 score = abs_score(a[j], zg);
-				const bool take = y < elems && (E & ~active) == 0 && score < best;
-				best = take ? score : best;
-				best_j = take ? j : best_j;
-			}
-		}
-		unsigned int best_e = 0xFFFFFFFFu;
-		if (best_j >= 0)
-		{
-			const unsigned int y = y0 + (best_j << 2);
-			best_e = ((y >> logw) << row_shift) | col_base | (y & wmask);
-		}
+			aborted = item(std::integral_constant<int, 0>{});
+		if (aborted)
+			return;
 		LatticeDev &L = wm_state(states, wm, li);
-		// Singleton (atom) masses live in block 0 and in the blocks whose
-		// first column is a power of two.
-		if (want_masses)
-		{
-#pragma unroll
-			for (int j = 0; j < kPerThread; j++)
-			{
-				const unsigned int y = y0 + (j << 2);
-				const unsigned int E = ((y >> logw) << row_shift) | col_base | (y & wmask);
-				if (y < elems && __popc(E) == 1)
-					L.atom_fixed[__ffs(E) - 1] = a[j];
-			}
-		}
 		argmin_block(best, best_e, ps.ws, ps.we); // (its barrier also publishes ps.flag)
 		issued = ps.flag != 0;
 		if (tid == 0)
