@@ -176,6 +176,7 @@ struct LatCache
 	u64 zg;
 	int s_g;
 	int masses;
+	int leaf_only;
 	u64 *tile_total;
 	int *tile_scale;
 	u64 *ftab;
@@ -835,6 +836,7 @@ __device__ __forceinline__ void fill_lattice_cache(const LatticeDev &L, int li, 
 			c.prior_hi = L.prior_hi;
 			c.zg = L.z_g;
 			c.masses = L.masses_in_k2;
+			c.leaf_only = L.leaf_only;
 			c.tile_total = L.tile_total;
 			c.tile_scale = L.tile_scale;
 			c.ftab = L.ftab;
@@ -849,6 +851,114 @@ __device__ __forceinline__ void load_lattice_cache(const LatticeDev &L, int li)
 {
 	if (threadIdx.x < 32)
 		fill_lattice_cache(L, li, ps.lc, threadIdx.x, true);
+}
+
+// The zeta threads' part of an item of a tree node at the depth limit: such a
+// node is a leaf and is never selected on, so of the 13-bit zeta only what
+// the epilogue reads is formed -- the tile total and the sums over each tile
+// bit (the zeta at the singleton columns), written where the zeta's stores
+// would put them.  In the phase-B layout tile bits 0..4 are lane bits, bit 5
+// and bits 10..12 warp bits and bits 6..9 register bits.
+template <typename T, bool kFull, typename Issue2>
+__device__ __forceinline__ void leaf_item(const ItemCfg &cfg, unsigned int r, int x, int scale, bool store_q,
+										  Issue2 &&issue2, u64 &total_out)
+{
+	T *const in = reinterpret_cast<T *>(tile_f64(x));
+	u64 *const work = work_tile();
+	const unsigned int tid = threadIdx.x;
+	const unsigned int lane = tid & 31u, warp = tid >> 5;
+	const int tbits = kFull ? kTileBits : cfg.tbits;
+	const unsigned int tsize = 1u << tbits;
+	const bool full = kFull || tsize == kTileElems;
+	const size_t base = static_cast<size_t>(r) << tbits;
+	if (store_q && tid == 0)
+	{
+		bulk_store(reinterpret_cast<T *>(cfg.q_out) + base, in, static_cast<uint32_t>(sizeof(T)) << tbits);
+		bulk_commit();
+	}
+	u64 a[kPerThread];
+#pragma unroll
+	for (int j = 0; j < kPerThread; j++)
+	{
+		const unsigned int xx = map_b(tid, j);
+		a[j] = (full || xx < tsize) ? to_fixed_fast(in[xx], scale) : 0ull;
+	}
+	// a[0]: this thread's sum; a[1 << k]: its sum over tile bit 6 + k set.
+	levels_b(a, tsize - 1u);
+	if (tid == 0)
+		bulk_wait_read_all();
+	zsync();
+	if (tid == 0)
+	{
+		mbar_arrive(&ps.freed[x]);
+		proxy_fence();
+		issue2();
+	}
+	// Superset sums over the lanes: lane 0 holds the warp's total, lane
+	// 1 << b the warp's sum over tile bit b.
+	u64 t = a[0];
+#pragma unroll
+	for (int b = 0; b < 5; b++)
+	{
+		const u64 o = __shfl_xor_sync(0xFFFFFFFFu, t, 1 << b);
+		if (!(lane & (1u << b)))
+			t += o;
+	}
+	u64 rk[4] = {a[1], a[2], a[4], a[8]};
+#pragma unroll
+	for (int k = 0; k < 4; k++)
+		for (int o = 16; o > 0; o >>= 1)
+			rk[k] += __shfl_xor_sync(0xFFFFFFFFu, rk[k], o);
+	// The work tile (unused by leaf items) holds the per-warp parts:
+	// [0, 16) warp totals, [16, 96) lane-bit sums, [96, 160) register-bit sums.
+	if (lane == 0)
+	{
+		work[warp] = t;
+#pragma unroll
+		for (int k = 0; k < 4; k++)
+			work[96 + warp * 4 + k] = rk[k];
+	}
+	else if ((lane & (lane - 1u)) == 0)
+		work[16 + warp * 5 + (__ffs(lane) - 1)] = t;
+	zsync();
+	// Thread b < 13 sums tile bit b over the warps, thread 13 the total: a
+	// lane-bit or register-bit part of every warp, or the totals of the
+	// warps whose index has the bit (tile bit 5 is warp bit 0, bits 10..12
+	// warp bits 1..3).
+	if (tid < 14)
+	{
+		int src, stride, sel;
+		if (tid < 5)
+			src = 16 + tid, stride = 5, sel = -1;
+		else if (tid < 6)
+			src = 0, stride = 1, sel = 0;
+		else if (tid < 10)
+			src = 96 + (tid - 6), stride = 4, sel = -1;
+		else if (tid < 13)
+			src = 0, stride = 1, sel = tid - 9;
+		else
+			src = 0, stride = 1, sel = -1;
+		u64 v = 0;
+#pragma unroll
+		for (int w = 0; w < kThreads / 32; w++)
+			if (sel < 0 || ((w >> sel) & 1))
+				v += work[src + w * stride];
+		work[160 + tid] = v;
+	}
+	zsync();
+	// Thread 0 stores them (its fence before the lattice's completion count
+	// publishes them to the epilogue).
+	if (tid == 0)
+	{
+		const size_t rows = size_t{1} << cfg.hbits;
+		for (int b = 0; b < tbits && b < 13; b++)
+		{
+			const unsigned int col = 1u << b;
+			cfg.m1[((static_cast<size_t>(col >> cfg.logw) * rows + r) * cfg.colw) + (col & (cfg.colw - 1))] =
+				work[160 + b];
+		}
+	}
+	total_out = work[173];
 }
 
 // The per-lattice constants of an item from a lattice cache (phi, the
@@ -1124,7 +1234,16 @@ __device__ void k1_zeta_role(LatticeDev *states, const WorkMap &wm, ItemRange ir
 		const ItemCfg cfg = item_cfg(ps.lc);
 		u64 tile_total = 0;
 		const bool full = cfg.tbits == kTileBits;
-		if (ps.lc.fp32)
+		if (ps.lc.leaf_only)
+		{
+			if (ps.lc.fp32)
+				leaf_item<float, false>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+			else if (full)
+				leaf_item<double, true>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+			else
+				leaf_item<double, false>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);
+		}
+		else if (ps.lc.fp32)
 		{
 			if (full)
 				zeta_item<float, true>(cfg, r, x, scale, mode != kLoad, issue2, tile_total);

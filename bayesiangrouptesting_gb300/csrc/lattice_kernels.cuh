@@ -166,6 +166,7 @@ struct LatticeDev
 	// ---- trees built on the device ----
 	TreeNodeRec *node;             // this node's record (nullptr: not a device-built tree node)
 	int node_stage, depth_limit;   // the node's depth and the search depth
+	int leaf_only;                 // a node at the depth limit: K1 writes only the atom sums, no zeta
 	alignas(64) unsigned char m1_map[128];
 };
 

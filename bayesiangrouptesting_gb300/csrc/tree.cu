@@ -248,6 +248,7 @@ __global__ void tree_expand(const LatticeDev *parents, LatticeDev *children, con
 	d.k1_count = 0;
 	d.k2_count = 0;
 	d.node_stage = P.node_stage + 1;
+	d.leaf_only = d.node_stage >= P.depth_limit ? 1 : 0;
 	children[c] = d;
 	TreeNodeRec nd;
 	nd.ex = P.best_e;
@@ -733,6 +734,7 @@ void build_tree_graph(TreeGraph &t)
 	root.node = t.recs;
 	root.node_stage = 0;
 	root.depth_limit = t.depth;
+	root.leaf_only = t.depth == 0 ? 1 : 0;
 	*t.h_root = root; // thresholds are filled per run
 	TreeNodeRec rr{};
 	rr.exists = 1;
