@@ -8,7 +8,7 @@ from conftest import assert_posterior_close
 
 pytestmark = pytest.mark.gpu
 
-RTOL = 1e-12  # FP64 posterior tolerance (SURVEY 8d / reference tests/cpp/support/assertions.hpp:14-19)
+RTOL = 1e-12  # FP64 posterior tolerance (the reference's tests/cpp/support/assertions.hpp:14-19)
 
 
 def _lattice(n, pi0, dilution=False):

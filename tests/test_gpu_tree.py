@@ -1,7 +1,7 @@
 """Tree simulation parity (bgt_cuda_provider_run through run_simulation)
 against the CPU oracle: the reference's CUDA parity cases
 (tests/cpp/integration/cuda_tree_parity_test.cpp:75-150), the single-subject
-golden (tests/cpp/support/assertions.hpp:80-92) and BASELINE-sized trees."""
+golden (tests/cpp/support/assertions.hpp:80-92) and seeded trees up to 16 subjects."""
 import numpy as np
 import pytest
 
