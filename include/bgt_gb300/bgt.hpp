@@ -1,8 +1,9 @@
 // C++20 host API of the GB300 provider, with the reference's public names:
 // bgt::Lattice (include/bgt/lattice.hpp:34-67), bgt::DilutionTable
 // (:17-32), bgt::TreeStats / SimulationOptions (include/bgt/types.hpp:81-130),
-// bgt::run_simulation for local trees (include/bgt/simulation.hpp:127) and
-// bgt::Error with bgt::StatusCode (include/bgt/status.hpp:10-60).  Code
+// bgt::run_simulation for local trees with its run report, progress snapshots
+// and cancellation (include/bgt/simulation.hpp:13-129) and bgt::Error with
+// bgt::StatusCode (include/bgt/status.hpp:10-60).  Code
 // written against the reference's bgt::Lattice compiles against this header
 // and runs on the device, through the C ABI of bgt_gpu.h and bgt_serve.h
 // (link libbgt_gb300.so).
@@ -15,8 +16,16 @@
 // src/core/lattice_api.cpp:17-26.
 #pragma once
 
+#include <atomic>
+#include <chrono>
 #include <cstdint>
+#include <filesystem>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <optional>
 #include <span>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -294,39 +303,439 @@ struct DilutionParameters
 	host_probability_t h = 0.005;
 };
 
-// The local_tree subset of bgt::SimulationConfig (include/bgt/simulation.hpp:87-103).
+// include/bgt/simulation.hpp:13-42.  Only local_tree is served here; the
+// parallel modes need the MPI backend.
+enum class SimulationMode
+{
+	local_tree,
+	parallel_global_tree,
+	parallel_dynamic_tree,
+	parallel_hybrid_tree,
+	parallel_partial_tree,
+	parallel_fusion_tree
+};
+
+enum class TrueStatePolicy
+{
+	all,
+	trimmed,
+	symmetric
+};
+
+enum class SimulationRunStatus
+{
+	completed,
+	interrupted,
+	running
+};
+
+enum class TerminationReason
+{
+	none,
+	user_signal,
+	cancellation_requested
+};
+
+// include/bgt/simulation.hpp:50-72.
+struct ReportConfig
+{
+	bool write_csv = false;
+	std::filesystem::path output_directory = ".";
+	std::string run_name;
+};
+
+struct SimulationTimings
+{
+	double setup_seconds = 0.0;
+	double tree_build_seconds = 0.0;
+	double evaluation_seconds = 0.0;
+	double total_seconds = 0.0;
+};
+
+struct ProgressConfig
+{
+	bool enabled = false;
+	double interval_seconds = 5.0;
+	std::filesystem::path output_path;
+	bool write_jsonl = true;
+	bool print_stderr = false;
+};
+
+// bgt::SimulationConfig (include/bgt/simulation.hpp:87-103).  As on the
+// reference's CUDA path, evaluation_prior, true_state_policy, trim_percent,
+// global_tree_depth and workload_granularity do not change a local_tree run on
+// the device (every true state is evaluated under the prior).
 struct SimulationConfig
 {
 	LatticeType lattice_type = LatticeType::replicated_non_dilution;
 	int subjects = 0;
 	int variants = 1;
 	std::vector<host_probability_t> prior;
+	std::optional<std::vector<host_probability_t>> evaluation_prior;
 	SimulationOptions options;
+	SimulationMode mode = SimulationMode::local_tree;
+	TrueStatePolicy true_state_policy = TrueStatePolicy::all;
+	int global_tree_depth = 0;
+	int workload_granularity = 1;
+	host_probability_t trim_percent = 1.0;
 	DilutionParameters dilution;
+	ReportConfig report;
+	ProgressConfig progress;
 };
 
+// bgt::SimulationResult (include/bgt/simulation.hpp:105-121), without the
+// KernelSpec.
 struct SimulationResult
 {
 	TreeStats stats;
-	Provider provider = Provider::cuda;
-	std::uint64_t total_states = 0;
-	std::uint64_t evaluated_states = 0;
+	SimulationMode mode = SimulationMode::local_tree;
+	Provider provider = Provider::auto_select;
+	int rank = 0;
+	int world_size = 1;
+	int total_states = 0;
+	int evaluated_states = 0;
+	std::string report_path;
+	SimulationTimings timings;
+	SimulationRunStatus status = SimulationRunStatus::completed;
+	TerminationReason termination_reason = TerminationReason::none;
+	host_probability_t evaluated_prior_mass = 0.0;
+	std::string progress_path;
 };
+
+// Cancellation (src/runtime/progress.cpp:82-108): the first request wins.
+namespace detail
+{
+inline std::atomic<int> cancel_reason{static_cast<int>(TerminationReason::none)};
+} // namespace detail
+
+inline void clear_simulation_cancellation()
+{
+	detail::cancel_reason.store(static_cast<int>(TerminationReason::none), std::memory_order_release);
+}
+
+inline void request_simulation_cancellation(TerminationReason reason = TerminationReason::cancellation_requested)
+{
+	if (reason == TerminationReason::none)
+		reason = TerminationReason::cancellation_requested;
+	int expected = static_cast<int>(TerminationReason::none);
+	detail::cancel_reason.compare_exchange_strong(expected, static_cast<int>(reason), std::memory_order_acq_rel);
+}
+
+inline bool simulation_cancellation_requested()
+{
+	return detail::cancel_reason.load(std::memory_order_acquire) != static_cast<int>(TerminationReason::none);
+}
+
+inline TerminationReason simulation_cancellation_reason()
+{
+	return static_cast<TerminationReason>(detail::cancel_reason.load(std::memory_order_acquire));
+}
+
+namespace detail
+{
+
+inline const char *mode_name(SimulationMode mode)
+{
+	switch (mode)
+	{
+	case SimulationMode::local_tree:
+		return "local_tree";
+	case SimulationMode::parallel_global_tree:
+		return "parallel_global_tree";
+	case SimulationMode::parallel_dynamic_tree:
+		return "parallel_dynamic_tree";
+	case SimulationMode::parallel_hybrid_tree:
+		return "parallel_hybrid_tree";
+	case SimulationMode::parallel_partial_tree:
+		return "parallel_partial_tree";
+	case SimulationMode::parallel_fusion_tree:
+		return "parallel_fusion_tree";
+	}
+	return "unknown";
+}
+
+inline const char *status_name(SimulationRunStatus status)
+{
+	switch (status)
+	{
+	case SimulationRunStatus::completed:
+		return "completed";
+	case SimulationRunStatus::interrupted:
+		return "interrupted";
+	case SimulationRunStatus::running:
+		return "running";
+	}
+	return "unknown";
+}
+
+inline const char *reason_name(TerminationReason reason)
+{
+	switch (reason)
+	{
+	case TerminationReason::none:
+		return "none";
+	case TerminationReason::user_signal:
+		return "user_signal";
+	case TerminationReason::cancellation_requested:
+		return "cancellation_requested";
+	}
+	return "unknown";
+}
+
+inline std::string run_name(const SimulationConfig &config)
+{
+	return config.report.run_name.empty() ? mode_name(config.mode) : config.report.run_name;
+}
+
+inline double seconds_since(std::chrono::steady_clock::time_point start)
+{
+	return std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+}
+
+} // namespace detail
+
+// The field,value report of a finished (or interrupted: .partial.csv) run,
+// or "" when none was asked for; the fields and their iostream formatting
+// follow write_report_if_requested (src/runtime/reporting.cpp:10-45).
+inline std::string write_report_if_requested(const SimulationConfig &config, const SimulationResult &result)
+{
+	if (!config.report.write_csv || result.rank != 0)
+		return {};
+	std::filesystem::create_directories(config.report.output_directory);
+	const bool partial = result.status == SimulationRunStatus::interrupted;
+	const std::filesystem::path path =
+		config.report.output_directory / (detail::run_name(config) + (partial ? ".partial.csv" : ".csv"));
+	std::ofstream out(path, std::ios::trunc);
+	const TreeStats &st = result.stats;
+	const SimulationTimings &tm = result.timings;
+	const double coverage = result.total_states == 0 ? 0.0
+													 : static_cast<double>(result.evaluated_states) /
+														   static_cast<double>(result.total_states);
+	out << "field,value\n"
+		<< "status," << detail::status_name(result.status) << '\n'
+		<< "termination_reason," << detail::reason_name(result.termination_reason) << '\n'
+		<< "is_partial," << (partial ? "true" : "false") << '\n'
+		<< "mode," << detail::mode_name(result.mode) << '\n'
+		<< "provider," << static_cast<int>(result.provider) << '\n'
+		<< "subjects," << config.subjects << '\n'
+		<< "variants," << config.variants << '\n'
+		<< "world_size," << result.world_size << '\n'
+		<< "total_states," << result.total_states << '\n'
+		<< "evaluated_states," << result.evaluated_states << '\n'
+		<< "state_coverage_fraction," << coverage << '\n'
+		<< "evaluated_prior_mass," << result.evaluated_prior_mass << '\n'
+		<< "progress_path," << result.progress_path << '\n'
+		<< "total_leaves," << st.total_leaves << '\n'
+		<< "correct_probability," << st.correct_probability << '\n'
+		<< "incorrect_probability," << st.incorrect_probability << '\n'
+		<< "false_positive_probability," << st.false_positive_probability << '\n'
+		<< "false_negative_probability," << st.false_negative_probability << '\n'
+		<< "unclassified_probability," << st.unclassified_probability << '\n'
+		<< "expected_stages," << st.expected_stages << '\n'
+		<< "expected_tests," << st.expected_tests << '\n'
+		<< "setup_seconds," << tm.setup_seconds << '\n'
+		<< "tree_build_seconds," << tm.tree_build_seconds << '\n'
+		<< "evaluation_seconds," << tm.evaluation_seconds << '\n'
+		<< "total_seconds," << tm.total_seconds << '\n';
+	return path.string();
+}
+
+namespace detail
+{
+
+inline std::string json_escape(const std::string &value)
+{
+	std::string out;
+	for (char ch : value)
+	{
+		switch (ch)
+		{
+		case '\\':
+			out += "\\\\";
+			break;
+		case '"':
+			out += "\\\"";
+			break;
+		case '\n':
+			out += "\\n";
+			break;
+		case '\r':
+			out += "\\r";
+			break;
+		case '\t':
+			out += "\\t";
+			break;
+		default:
+			out += ch;
+		}
+	}
+	return out;
+}
+
+// The progress snapshots of a device run (ProgressTracker,
+// src/runtime/progress.cpp:139-300): a running snapshot before the tree is
+// launched and the final one after it.  Latest record in <run>.progress.json
+// (or the configured path), history in the same name with .jsonl.
+class ProgressTracker
+{
+  public:
+	ProgressTracker(const SimulationConfig &config, int rank, int total_states,
+					std::chrono::steady_clock::time_point start)
+		: config_(config), rank_(rank), total_states_(total_states), start_(start), last_emit_(start)
+	{
+		if (enabled())
+			path_ = latest_path().string();
+	}
+
+	const std::string &progress_path() const { return path_; }
+
+	void replace_state(int evaluated_states, double prior_mass, const TreeStats &stats)
+	{
+		const int known = stats_.total_leaves;
+		evaluated_ = evaluated_states;
+		prior_mass_ = prior_mass;
+		stats_ = stats;
+		if (stats_.total_leaves == 0)
+			stats_.total_leaves = known;
+	}
+
+	void maybe_emit(const std::string &message, bool force)
+	{
+		if (!enabled())
+			return;
+		const auto now = std::chrono::steady_clock::now();
+		if (!force && std::chrono::duration<double>(now - last_emit_).count() < config_.progress.interval_seconds)
+			return;
+		const TerminationReason reason = simulation_cancellation_reason();
+		write(reason == TerminationReason::none ? SimulationRunStatus::running : SimulationRunStatus::interrupted,
+			  reason, message);
+		last_emit_ = now;
+	}
+
+	void finish(SimulationRunStatus status, TerminationReason reason, const std::string &message)
+	{
+		if (enabled())
+			write(status, reason, message);
+	}
+
+  private:
+	bool enabled() const { return config_.progress.enabled && rank_ == 0; }
+
+	std::filesystem::path latest_path() const
+	{
+		if (!config_.progress.output_path.empty())
+			return config_.progress.output_path;
+		return config_.report.output_directory / (run_name(config_) + ".progress.json");
+	}
+
+	void write(SimulationRunStatus status, TerminationReason reason, const std::string &message) const
+	{
+		const double elapsed = seconds_since(start_);
+		const double coverage =
+			total_states_ == 0 ? 0.0 : static_cast<double>(evaluated_) / static_cast<double>(total_states_);
+		std::ostringstream body;
+		body << std::setprecision(17) << "{\"status\":\"" << status_name(status) << "\",\"termination_reason\":\""
+			 << reason_name(reason) << "\",\"total_states\":" << total_states_ << ",\"evaluated_states\":" << evaluated_
+			 << ",\"state_coverage_fraction\":" << coverage << ",\"evaluated_prior_mass\":" << prior_mass_
+			 << ",\"stats\":{\"total_leaves\":" << stats_.total_leaves
+			 << ",\"correct_probability\":" << stats_.correct_probability
+			 << ",\"incorrect_probability\":" << stats_.incorrect_probability
+			 << ",\"false_positive_probability\":" << stats_.false_positive_probability
+			 << ",\"false_negative_probability\":" << stats_.false_negative_probability
+			 << ",\"unclassified_probability\":" << stats_.unclassified_probability
+			 << ",\"expected_stages\":" << stats_.expected_stages << ",\"expected_tests\":" << stats_.expected_tests
+			 << "},\"timings\":{\"setup_seconds\":0,\"tree_build_seconds\":0,\"evaluation_seconds\":0,"
+			 << "\"total_seconds\":" << elapsed << "},\"message\":\"" << json_escape(message) << "\"}";
+		const std::filesystem::path latest = latest_path();
+		if (!latest.parent_path().empty())
+			std::filesystem::create_directories(latest.parent_path());
+		const std::filesystem::path tmp = latest.string() + ".tmp";
+		{
+			std::ofstream out(tmp, std::ios::trunc);
+			out << body.str() << '\n';
+		}
+		std::filesystem::rename(tmp, latest);
+		if (config_.progress.write_jsonl)
+		{
+			std::filesystem::path history = latest;
+			history.replace_extension(".jsonl");
+			std::ofstream out(history, std::ios::app);
+			out << body.str() << '\n';
+		}
+		if (config_.progress.print_stderr)
+		{
+			std::cerr << "bgt progress: status=" << status_name(status) << " evaluated=" << evaluated_ << '/'
+					  << total_states_ << " coverage=" << coverage << " prior_mass=" << prior_mass_
+					  << " elapsed=" << elapsed << "s";
+			if (!message.empty())
+				std::cerr << " " << message;
+			std::cerr << '\n';
+		}
+	}
+
+	const SimulationConfig &config_;
+	int rank_;
+	int total_states_;
+	std::chrono::steady_clock::time_point start_, last_emit_;
+	int evaluated_ = 0;
+	double prior_mass_ = 0.0;
+	TreeStats stats_{};
+	std::string path_;
+};
+
+} // namespace detail
 
 inline bool cuda_available() { return bgt_cuda_provider_available() != 0; }
 
 // bgt::run_simulation for local trees on the device (Runtime::run_simulation,
-// src/runtime/simulation_runner.cpp:181-262, through CudaProvider::run).
+// src/runtime/simulation_runner.cpp:181-262, through CudaProvider::run):
+// validation, cancellation before evaluation, progress snapshots, the run
+// and the CSV report.
 inline SimulationResult run_simulation(const SimulationConfig &config)
 {
+	const auto total_start = std::chrono::steady_clock::now();
 	const SimulationOptions &o = config.options;
+	const int atoms = config.subjects * config.variants;
 	if (config.subjects <= 0 || config.variants <= 0 || o.search_depth < 0)
 		throw Error(StatusCode::invalid_argument, "invalid simulation dimensions.");
-	if (config.prior.size() != static_cast<std::size_t>(config.subjects) * static_cast<std::size_t>(config.variants))
+	if (config.workload_granularity <= 0)
+		throw Error(StatusCode::invalid_argument, "workload_granularity must be positive.");
+	if (config.progress.interval_seconds <= 0.0)
+		throw Error(StatusCode::invalid_argument, "progress interval must be positive.");
+	if (config.prior.size() != static_cast<std::size_t>(atoms))
 		throw Error(StatusCode::invalid_argument, "prior length must equal subjects * variants.");
+	if (config.evaluation_prior && config.evaluation_prior->size() != static_cast<std::size_t>(atoms))
+		throw Error(StatusCode::invalid_argument, "evaluation_prior length must equal subjects * variants.");
+	if (config.lattice_type == LatticeType::distributed_non_dilution ||
+		config.lattice_type == LatticeType::distributed_dilution)
+		throw Error(StatusCode::invalid_argument, "local_tree requires a replicated lattice.");
+	if (config.mode != SimulationMode::local_tree)
+		throw Error(StatusCode::unsupported,
+					"parallel simulation modes need the MPI backend; the GB300 provider serves local_tree on one GPU.");
 	if (o.provider == Provider::cpu)
 		throw Error(StatusCode::unsupported, "the CPU provider is the reference library's.");
 	const bool dil = detail::uses_dilution(config.lattice_type);
+	if (dil && (config.dilution.alpha <= 0.0 || config.dilution.h <= 0.0))
+		throw Error(StatusCode::invalid_argument, "dilution parameters must be positive.");
+
+	SimulationResult r;
+	r.mode = config.mode;
+	r.total_states = atoms >= 31 ? 0 : (1 << atoms);
+	detail::ProgressTracker progress(config, r.rank, r.total_states, total_start);
+	const auto eval_start = std::chrono::steady_clock::now();
+	if (simulation_cancellation_requested())
+	{
+		r.status = SimulationRunStatus::interrupted;
+		r.termination_reason = simulation_cancellation_reason();
+		r.progress_path = progress.progress_path();
+		r.timings.total_seconds = detail::seconds_since(total_start);
+		progress.finish(r.status, r.termination_reason, "cancelled before evaluation started");
+		r.report_path = write_report_if_requested(config, r);
+		return r;
+	}
+	if (!cuda_available())
+		throw Error(StatusCode::cuda_error, "CUDA provider requested, but no CUDA device is available.");
+	progress.maybe_emit("starting CUDA evaluation", true);
 	DilutionTable table;
 	if (dil)
 		table = DilutionTable(config.subjects, config.dilution.alpha, config.dilution.h);
@@ -334,7 +743,6 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 	detail::check(bgt_cuda_provider_run(dil ? 1 : 0, config.subjects, config.variants, config.prior.data(),
 										o.search_depth, o.threshold_up, o.threshold_lo, o.branch_threshold,
 										static_cast<int>(o.selector), dil ? table.rows() : nullptr, &st));
-	SimulationResult r;
 	r.stats = TreeStats{st.total_leaves,
 						st.correct_probability,
 						st.incorrect_probability,
@@ -343,7 +751,15 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 						st.unclassified_probability,
 						st.expected_stages,
 						st.expected_tests};
-	r.total_states = r.evaluated_states = std::uint64_t{1} << (config.subjects * config.variants);
+	r.provider = Provider::cuda;
+	r.evaluated_states = r.total_states;
+	r.evaluated_prior_mass = 1.0;
+	progress.replace_state(r.evaluated_states, r.evaluated_prior_mass, r.stats);
+	r.timings.evaluation_seconds = detail::seconds_since(eval_start);
+	r.timings.total_seconds = detail::seconds_since(total_start);
+	r.progress_path = progress.progress_path();
+	progress.finish(r.status, r.termination_reason, "completed");
+	r.report_path = write_report_if_requested(config, r);
 	return r;
 }
 

@@ -2,11 +2,16 @@
 // C++ pins: tests/cpp/unit/lattice_api_test.cpp:63-99 (public order, upset
 // masses, selections, update, classification, multinomial BBPA = brute
 // force), tests/cpp/unit/dilution_test.cpp:11-13 (table rows) and the
-// single-subject TreeStats golden of tests/cpp/support/assertions.hpp:80-92.
+// single-subject TreeStats golden of tests/cpp/support/assertions.hpp:80-92,
+// plus the run report and progress files of run_simulation
+// (src/runtime/reporting.cpp:10-45).  argv[1]: a scratch directory.
 // Exit status 0 = pass; prints "skip" without a device.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <filesystem>
+#include <fstream>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -88,9 +93,39 @@ bgt::state_t brute_force_bbpa(const bgt::Lattice &lat, int n, int k)
 	return best_e;
 }
 
+std::map<std::string, std::string> read_report(const std::filesystem::path &path)
+{
+	std::map<std::string, std::string> rows;
+	std::ifstream in(path);
+	std::string line;
+	std::getline(in, line);
+	if (line != "field,value")
+	{
+		std::printf("FAIL report header: %s\n", line.c_str());
+		failures++;
+	}
+	while (std::getline(in, line))
+	{
+		const auto comma = line.find(',');
+		rows[line.substr(0, comma)] = line.substr(comma + 1);
+	}
+	return rows;
+}
+
+void expect_field(const std::map<std::string, std::string> &rows, const char *key, const char *want)
+{
+	const auto it = rows.find(key);
+	if (it == rows.end() || it->second != want)
+	{
+		std::printf("FAIL report %s: got '%s' want '%s'\n", key, it == rows.end() ? "(missing)" : it->second.c_str(),
+					want);
+		failures++;
+	}
+}
+
 } // namespace
 
-int main()
+int main(int argc, char **argv)
 {
 	if (!bgt::cuda_available())
 	{
@@ -153,6 +188,39 @@ int main()
 	expect_near(st.unclassified_probability, 0.206, 1e-12, "single-subject unclassified");
 	expect_near(st.expected_stages, 1.0, 1e-12, "single-subject expected stages");
 	expect_near(st.expected_tests, 1.0, 1e-12, "single-subject expected tests");
+
+	// Reports and progress files.
+	const std::filesystem::path dir =
+		argc > 1 ? std::filesystem::path(argv[1]) : std::filesystem::temp_directory_path() / "bgt_api_test";
+	cfg.report.write_csv = true;
+	cfg.report.output_directory = dir;
+	cfg.report.run_name = "single";
+	cfg.progress.enabled = true;
+	const bgt::SimulationResult res = bgt::run_simulation(cfg);
+	expect_equal(res.report_path == (dir / "single.csv").string(), 1, "report path");
+	const auto rows = read_report(res.report_path);
+	expect_field(rows, "status", "completed");
+	expect_field(rows, "is_partial", "false");
+	expect_field(rows, "mode", "local_tree");
+	expect_field(rows, "provider", "2");
+	expect_field(rows, "total_states", "2");
+	expect_field(rows, "evaluated_states", "2");
+	expect_field(rows, "state_coverage_fraction", "1");
+	expect_field(rows, "total_leaves", "2");
+	expect_field(rows, "correct_probability", "0.792");
+	expect_field(rows, "unclassified_probability", "0.206");
+	expect_field(rows, "expected_tests", "1");
+	expect_equal(std::filesystem::exists(dir / "single.progress.json"), 1, "progress file");
+	expect_equal(std::filesystem::exists(dir / "single.progress.jsonl"), 1, "progress history");
+	bgt::request_simulation_cancellation();
+	cfg.report.run_name = "cancelled";
+	const bgt::SimulationResult cancelled = bgt::run_simulation(cfg);
+	bgt::clear_simulation_cancellation();
+	expect_equal(cancelled.status == bgt::SimulationRunStatus::interrupted, 1, "cancelled status");
+	expect_equal(cancelled.report_path == (dir / "cancelled.partial.csv").string(), 1, "partial report path");
+	expect_field(read_report(cancelled.report_path), "termination_reason", "cancellation_requested");
+	cfg.mode = bgt::SimulationMode::parallel_global_tree;
+	expect_error([&] { bgt::run_simulation(cfg); }, bgt::StatusCode::unsupported, "parallel mode");
 
 	std::printf("%s (%d failures)\n", failures ? "FAIL" : "ok", failures);
 	return failures ? 1 : 0;

@@ -34,6 +34,6 @@ def test_cpp_api_compiles(tmp_path):
 @pytest.mark.gpu
 def test_cpp_api_reference_pins(gpu, tmp_path):
     exe = _compile(tmp_path, link=True)
-    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    out = subprocess.run([str(exe), str(tmp_path / "reports")], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.strip().startswith("ok"), out.stdout
