@@ -127,3 +127,23 @@ def test_rejects_unsupported_requests(gpu):
             srv.submit(SessionRequest(25, np.full(25, 0.1), 0, 1, 1))
         with pytest.raises(bgt.Error):
             srv.submit(SessionRequest(24, np.full(24, 0.1), 0, 1, 1))  # 256 MB + > budget
+
+
+def test_fp32_served_sessions_equal_fp32_plain_loop(gpu):
+    # FP32 storage: a served session is the same session as the one-session
+    # device loop on an FP32 lattice (same fixed-point sums, same draws).
+    reqs = _requests(16, seed=23, n_lo=8, n_hi=16)
+    with Server(GB, fp32=True) as srv:
+        tickets = [srv.submit(r) for r in reqs]
+        srv.run_until_idle()
+        served = [srv.result(t) for t in tickets]
+    for i in (0, 3, 9, 15):
+        q, r = reqs[i], served[i]
+        t = bgt.LatticeType.replicated_dilution if q.dilution else bgt.LatticeType.replicated_non_dilution
+        lat = bgt.Lattice(t, q.subjects, q.prior, precision=bgt.Precision.float32)
+        plain = lat.run_session_until_classified(MAX_STAGES, q.true_state, seed=q.seed, session=q.session,
+                                                 selector=bgt.SelectorType.auto_select, alpha=q.alpha, h=q.h)
+        assert r.error == 0 and plain["stages"] == r.stages
+        np.testing.assert_array_equal(plain["experiments"], r.experiments)
+        np.testing.assert_array_equal(plain["pos"], r.pos_masks)
+        np.testing.assert_array_equal(plain["neg"], r.neg_masks)

@@ -90,3 +90,23 @@ def test_leaf_sums_equal_true_state_sweep(gpu, dil, n, k, depth):
     leaf = _run(dil, n, pi0, depth, k=k)
     sweep = _run(dil, n, pi0, depth, branch=1e-300, k=k)
     _check(leaf, sweep)
+
+
+@pytest.mark.parametrize("dil,n", [(False, 3), (True, 14)])
+def test_depth_zero_tree_is_the_root(gpu, oracle, dil, n):
+    # Search depth 0: the root is the only (leaf-only) node.
+    pi0 = np.linspace(0.02, 0.2, n)
+    got = _run(dil, n, pi0, 0)
+    want = oracle.run_simulation(1 if dil else 0, n, 1, pi0, 0)
+    _check(got, want)
+
+
+@pytest.mark.parametrize("n,depth", [(14, 3), (13, 2), (9, 5)])
+def test_leaf_only_last_level_matches_oracle(gpu, oracle, n, depth):
+    # Trees whose last level has full (n >= 13) and partial tiles: the
+    # leaf-only items write the atom sums the classification reads.
+    rng = np.random.default_rng(300 + n)
+    pi0 = rng.uniform(0.05, 0.3, n)
+    got = _run(True, n, pi0, depth, up=0.05, lo=0.05)
+    want = oracle.run_simulation(1, n, 1, pi0, depth, 0.05, 0.05)
+    _check(got, want)
