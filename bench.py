@@ -167,14 +167,16 @@ def _oracle_worker(args):
     pi0 = session_prior(SEED, session)
     truth = session_truth(SEED, session, pi0)
     t0 = time.perf_counter()
-    o.session(1, SUBJECTS, 1, pi0, stages, SEED, session, truth, selector=2, alpha=ALPHA, h=H, up=THRESHOLD,
-              lo=THRESHOLD)
-    return stages, time.perf_counter() - t0
+    out = o.session(1, SUBJECTS, 1, pi0, stages, SEED, session, truth, selector=2, alpha=ALPHA, h=H, up=THRESHOLD,
+                    lo=THRESHOLD)
+    wall = time.perf_counter() - t0
+    return stages, wall, {key: np.asarray(out[key]).tolist() for key in ("experiments", "responses", "pos", "neg")}
 
 
-def cpu_baseline(stages: int = 2, workers: int = 1):
+def cpu_baseline(stages: int = 2, workers: int = 1, outputs: list = None):
     """The oracle port timed on host cores: `workers` independent sessions of
-    `stages` stages each, in parallel processes.  Returns stages/s."""
+    `stages` stages each, in parallel processes.  Returns stages/s and the
+    wall time; `outputs` (when given) receives each session's oracle stages."""
     from oracle.oracle import build_oracle
 
     build_oracle()
@@ -187,7 +189,25 @@ def cpu_baseline(stages: int = 2, workers: int = 1):
         with ctx.Pool(workers) as pool:
             results = pool.map(_oracle_worker, jobs)
     wall = time.perf_counter() - t0
+    if outputs is not None:
+        outputs.extend((jobs[i][0], r[2]) for i, r in enumerate(results))
     return sum(r[0] for r in results) / wall, wall
+
+
+def session_parity(session: int, want: dict) -> dict:
+    """The same session on the device (through the package's Lattice API):
+    whether its stages equal the oracle's."""
+    import bayesiangrouptesting_gb300 as bgt
+
+    pi0 = session_prior(SEED, session)
+    truth = session_truth(SEED, session, pi0)
+    stages = len(want["experiments"])
+    lat = bgt.Lattice(bgt.LatticeType.replicated_dilution, SUBJECTS, pi0)
+    got = lat.run_session(stages, truth, seed=SEED, session=session, selector=bgt.SelectorType.op_bbpa, alpha=ALPHA,
+                          h=H, threshold_up=THRESHOLD, threshold_lo=THRESHOLD)
+    same = all(np.array_equal(np.asarray(got[k], dtype=np.uint32), np.asarray(want[k], dtype=np.uint32))
+               for k in ("experiments", "responses", "pos", "neg"))
+    return {"session": session, "stages_compared": stages, "identical_to_oracle": bool(same)}
 
 
 def read_profile_traffic():
@@ -572,9 +592,11 @@ def run_gpu(args, world, rank, local):
                                  "run right after the timed region (kept out of it so they do not perturb it)"}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cv, cwall = cpu_baseline(stages=args.cpu_stages, workers=1)
+        oracle_out = []
+        cv, cwall = cpu_baseline(stages=args.cpu_stages, workers=1, outputs=oracle_out)
         cpu = {"value": cv, "unit": "stages/s", "cores": 1, "kind": "port",
-               "sample": f"one n=24 session, {args.cpu_stages} stages, oracle port on 1 core ({cwall:.1f} s)"}
+               "sample": f"one n=24 session, {args.cpu_stages} stages, oracle port on 1 core ({cwall:.1f} s)",
+               "parity": session_parity(*oracle_out[0])}
     precision = None
     if rank == 0 and world == 1 and not args.no_precision:
         precision = run_precision()
