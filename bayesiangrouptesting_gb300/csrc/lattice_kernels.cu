@@ -1824,6 +1824,14 @@ __global__ void __launch_bounds__(kThreads, 2) k2_zeta_high_select(LatticeDev *s
 			aborted = item(std::integral_constant<int, 3>{});
 		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 4)
 			aborted = item(std::integral_constant<int, 4>{});
+		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 5)
+			aborted = item(std::integral_constant<int, 5>{});
+		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 6)
+			aborted = item(std::integral_constant<int, 6>{});
+		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 7)
+			aborted = item(std::integral_constant<int, 7>{});
+		else if (elems_rt == static_cast<unsigned int>(kTileElems) && logw_rt == 8)
+			aborted = item(std::integral_constant<int, 8>{});
 		else
 			aborted = item(std::integral_constant<int, 0>{});
 		if (aborted)
