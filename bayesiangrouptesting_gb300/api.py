@@ -172,6 +172,51 @@ class TreeStats:
                          self.unclassified_probability, self.expected_stages, self.expected_tests])
 
 
+class OptimizationLevel(enum.IntEnum):
+    """bgt::OptimizationLevel (include/bgt/compile_options.hpp:11-16)."""
+
+    debug = 0
+    release = 1
+    aggressive = 2
+
+
+class ProfileBackend(enum.IntEnum):
+    """bgt::ProfileBackend (include/bgt/compile_options.hpp:24-28)."""
+
+    none = 0
+    caliper = 1
+
+
+class DilutionMode(enum.IntEnum):
+    """bgt::DilutionMode (include/bgt/types.hpp:103-107)."""
+
+    non_dilution = 0
+    dilution = 1
+
+
+@dataclass
+class CompileOptions:
+    """bgt::CompileOptions (include/bgt/compile_options.hpp:56-93).  The device
+    kernels are built ahead of time for sm_103a; the options are kept so that
+    code setting them runs unchanged, and enable_cuda=False refuses
+    Provider.cuda as the reference does."""
+
+    enable_simd: bool = False
+    enable_openmp: bool = False
+    enable_cuda: bool = True
+    enable_nccl: bool = False
+    enable_nccl_gin: bool = False
+    fast_math: bool = False
+    native_cpu: bool = False
+    posterior_precision: Precision = Precision.float64
+    accumulator_precision: Precision = Precision.float64
+    optimization: OptimizationLevel = OptimizationLevel.release
+    profile_backend: ProfileBackend = ProfileBackend.none
+    extra_cxx_flags: list = field(default_factory=list)
+    extra_cuda_flags: list = field(default_factory=list)
+    definitions: list = field(default_factory=list)
+
+
 @dataclass
 class SimulationOptions:
     """bgt::SimulationOptions (include/bgt/types.hpp:121-130)."""
@@ -182,6 +227,34 @@ class SimulationOptions:
     branch_threshold: float = 0.0
     selector: SelectorType = SelectorType.auto_select
     provider: Provider = Provider.auto_select
+    compile_options: CompileOptions = field(default_factory=CompileOptions)
+
+
+@dataclass
+class KernelSpec:
+    """bgt::KernelSpec (include/bgt/types.hpp:132-181): what a run asks for."""
+
+    provider: Provider = Provider.auto_select
+    subjects: int = 0
+    variants: int = 1
+    state_bits: int = 32
+    dilution: DilutionMode = DilutionMode.non_dilution
+    selector: SelectorType = SelectorType.auto_select
+    precision: Precision = Precision.float64
+    accumulator_precision: Precision = Precision.float64
+    cuda_arch: str = "sm_103a"
+    compile_options: CompileOptions = field(default_factory=CompileOptions)
+
+
+@dataclass
+class JitCacheInfo:
+    """bgt::JitCacheInfo (include/bgt/types.hpp:183-189): always empty here
+    (no run-time compilation)."""
+
+    memory_entries: int = 0
+    disk_entries: int = 0
+    disk_cache_directory: str = ""
+    jit_enabled: bool = False
 
 
 @dataclass
@@ -291,6 +364,7 @@ class SimulationResult:
     total_states: int
     evaluated_states: int
     mode: SimulationMode = SimulationMode.local_tree
+    kernel: KernelSpec = field(default_factory=KernelSpec)
     rank: int = 0
     world_size: int = 1
     report_path: str = ""
@@ -343,6 +417,70 @@ def available_providers():
     return [Provider.cpu] + ([Provider.cuda] if cuda_available() else [])
 
 
+def make_kernel_spec(config: "SimulationConfig") -> KernelSpec:
+    """Runtime::make_kernel_spec (src/runtime/simulation_runner.cpp:166-179)."""
+    co = config.options.compile_options
+    return KernelSpec(provider=config.options.provider, subjects=config.subjects, variants=config.variants,
+                      dilution=DilutionMode.dilution if _uses_dilution(config.lattice_type) else DilutionMode.non_dilution,
+                      selector=_resolve_selector(config.options.selector, config.variants),
+                      precision=co.posterior_precision, accumulator_precision=co.accumulator_precision,
+                      compile_options=co)
+
+
+def jit_cache_info() -> JitCacheInfo:
+    return JitCacheInfo()
+
+
+def clear_jit_cache() -> None:
+    """No run-time compilation here: nothing to clear."""
+
+
+class Runtime:
+    """bgt::Runtime (include/bgt/runtime.hpp:58-74) without run-time
+    compilation: the kernels are built ahead of time for sm_103a."""
+
+    def __init__(self, cache_directory: str = ""):
+        self.cache_directory = str(cache_directory)
+
+    def available_providers(self):
+        return available_providers()
+
+    def jit_cache_info(self) -> JitCacheInfo:
+        return JitCacheInfo(disk_cache_directory=self.cache_directory)
+
+    def clear_jit_cache(self) -> None:
+        clear_jit_cache()
+
+    def make_kernel_spec(self, config: "SimulationConfig") -> KernelSpec:
+        return make_kernel_spec(config)
+
+    def run_simulation(self, config: "SimulationConfig") -> "SimulationResult":
+        return run_simulation(config)
+
+
+class CudaProvider:
+    """bgt::CudaProvider (include/bgt/runtime.hpp:50-56): one tree simulation
+    through bgt_cuda_provider_run."""
+
+    def available(self) -> bool:
+        return cuda_available()
+
+    def run(self, type: LatticeType, subjects: int, variants: int, prior, options: SimulationOptions,
+            dilution: "Optional[DilutionTable]" = None) -> TreeStats:
+        prior = np.ascontiguousarray(prior, dtype=np.float64)
+        if prior.size != subjects * variants:
+            raise ValueError("prior length must equal subjects * variants.")
+        dil = _uses_dilution(type)
+        if dil and dilution is None:
+            raise ValueError("dilution table is required for dilution models.")
+        stats = TreeStatsC()
+        _call(load().bgt_cuda_provider_run(1 if dil else 0, subjects, variants, prior.ctypes.data_as(_dp),
+                                           options.search_depth, options.threshold_up, options.threshold_lo,
+                                           options.branch_threshold, int(options.selector),
+                                           dilution.rows() if dil else None, ctypes.byref(stats)))
+        return TreeStats.from_c(stats)
+
+
 def _validate(config: SimulationConfig) -> None:
     """validate_simulation_config, src/runtime/simulation_runner.cpp:30-68."""
     o = config.options
@@ -380,8 +518,11 @@ def run_simulation(config: SimulationConfig) -> SimulationResult:
     _validate(config)
     if config.options.provider == Provider.cpu:
         raise Error(StatusCode.unsupported, "the CPU provider is the reference library's; this package is the CUDA provider")
+    if config.options.provider == Provider.cuda and not config.options.compile_options.enable_cuda:
+        raise Error(StatusCode.unsupported, "CUDA provider requested, but CUDA is disabled in compile options.")
     total = 1 << (config.subjects * config.variants)
-    result = SimulationResult(TreeStats(), Provider.auto_select, total, 0, mode=config.mode)
+    result = SimulationResult(TreeStats(), Provider.auto_select, total, 0, mode=config.mode,
+                              kernel=make_kernel_spec(config))
     progress = ProgressTracker(config, result.rank, result.total_states, total_start)
     eval_start = time.perf_counter()
     if simulation_cancellation_requested():
@@ -409,6 +550,7 @@ def run_simulation(config: SimulationConfig) -> SimulationResult:
     _call(status)
     result.stats = TreeStats.from_c(stats)
     result.provider = Provider.cuda
+    result.kernel.provider = Provider.cuda
     result.evaluated_states = total
     result.evaluated_prior_mass = 1.0
     progress.replace_state(result.evaluated_states, result.evaluated_prior_mass, result.stats)

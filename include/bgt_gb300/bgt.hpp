@@ -68,6 +68,49 @@ enum class Precision
 	float64
 };
 
+// include/bgt/compile_options.hpp:11-93 and include/bgt/types.hpp:103-107.
+// The device kernels are compiled once for sm_103a; CompileOptions and
+// KernelSpec are kept so that code building them compiles unchanged, and a
+// KernelSpec records what a run asked for.
+enum class OptimizationLevel
+{
+	debug,
+	release,
+	aggressive
+};
+
+enum class ProfileBackend
+{
+	none,
+	caliper
+};
+
+enum class DilutionMode
+{
+	non_dilution,
+	dilution
+};
+
+struct CompileOptions
+{
+	bool enable_simd = false;
+	bool enable_openmp = false;
+	bool enable_cuda = true;
+	bool enable_nccl = false;
+	bool enable_nccl_gin = false;
+	bool fast_math = false;
+	bool native_cpu = false;
+	Precision posterior_precision = Precision::float64;
+	Precision accumulator_precision = Precision::float64;
+	OptimizationLevel optimization = OptimizationLevel::release;
+	ProfileBackend profile_backend = ProfileBackend::none;
+	std::vector<std::string> extra_cxx_flags;
+	std::vector<std::string> extra_cuda_flags;
+	std::vector<std::string> definitions;
+
+	bool operator==(const CompileOptions &) const = default;
+};
+
 enum class StatusCode
 {
 	success,
@@ -295,6 +338,7 @@ struct SimulationOptions
 	double branch_threshold = 0.0;
 	SelectorType selector = SelectorType::auto_select;
 	Provider provider = Provider::auto_select;
+	CompileOptions compile_options;
 };
 
 struct DilutionParameters
@@ -383,11 +427,57 @@ struct SimulationConfig
 	ProgressConfig progress;
 };
 
-// bgt::SimulationResult (include/bgt/simulation.hpp:105-121), without the
-// KernelSpec.
+// bgt::KernelSpec (include/bgt/types.hpp:132-181): what a run asks for.
+struct KernelSpec
+{
+	Provider provider = Provider::auto_select;
+	int subjects = 0;
+	int variants = 1;
+	int state_bits = 32;
+	DilutionMode dilution = DilutionMode::non_dilution;
+	SelectorType selector = SelectorType::auto_select;
+	Precision precision = Precision::float64;
+	Precision accumulator_precision = Precision::float64;
+	std::string cuda_arch = "sm_103a";
+	CompileOptions compile_options;
+
+	bool operator==(const KernelSpec &) const = default;
+};
+
+struct KernelSpecHash
+{
+	std::size_t operator()(const KernelSpec &spec) const
+	{
+		std::size_t seed = 0;
+		auto mix = [&seed](std::size_t v) { seed ^= v + 0x9e3779b9u + (seed << 6) + (seed >> 2); };
+		mix(static_cast<std::size_t>(spec.provider));
+		mix(static_cast<std::size_t>(spec.subjects));
+		mix(static_cast<std::size_t>(spec.variants));
+		mix(static_cast<std::size_t>(spec.state_bits));
+		mix(static_cast<std::size_t>(spec.dilution));
+		mix(static_cast<std::size_t>(spec.selector));
+		mix(static_cast<std::size_t>(spec.precision));
+		mix(static_cast<std::size_t>(spec.accumulator_precision));
+		mix(std::hash<std::string>{}(spec.cuda_arch));
+		return seed;
+	}
+};
+
+// bgt::JitCacheInfo (include/bgt/types.hpp:183-189): no run-time compilation
+// here, so always empty and disabled.
+struct JitCacheInfo
+{
+	std::size_t memory_entries = 0;
+	std::size_t disk_entries = 0;
+	std::string disk_cache_directory;
+	bool jit_enabled = false;
+};
+
+// bgt::SimulationResult (include/bgt/simulation.hpp:105-121).
 struct SimulationResult
 {
 	TreeStats stats;
+	KernelSpec kernel;
 	SimulationMode mode = SimulationMode::local_tree;
 	Provider provider = Provider::auto_select;
 	int rank = 0;
@@ -687,6 +777,34 @@ class ProgressTracker
 
 inline bool cuda_available() { return bgt_cuda_provider_available() != 0; }
 
+namespace detail
+{
+
+// resolve_selector (src/runtime/simulation_helpers.cpp:40-45).
+inline SelectorType resolve_selector(SelectorType selector, int variants)
+{
+	if (selector != SelectorType::auto_select)
+		return selector;
+	return variants == 1 ? SelectorType::op_bha : SelectorType::op_bbpa;
+}
+
+// Runtime::make_kernel_spec (src/runtime/simulation_runner.cpp:166-179).
+inline KernelSpec kernel_spec(const SimulationConfig &config)
+{
+	KernelSpec spec;
+	spec.provider = config.options.provider;
+	spec.subjects = config.subjects;
+	spec.variants = config.variants;
+	spec.dilution = uses_dilution(config.lattice_type) ? DilutionMode::dilution : DilutionMode::non_dilution;
+	spec.selector = resolve_selector(config.options.selector, config.variants);
+	spec.compile_options = config.options.compile_options;
+	spec.precision = config.options.compile_options.posterior_precision;
+	spec.accumulator_precision = config.options.compile_options.accumulator_precision;
+	return spec;
+}
+
+} // namespace detail
+
 // bgt::run_simulation for local trees on the device (Runtime::run_simulation,
 // src/runtime/simulation_runner.cpp:181-262, through CudaProvider::run):
 // validation, cancellation before evaluation, progress snapshots, the run
@@ -718,7 +836,10 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 	if (dil && (config.dilution.alpha <= 0.0 || config.dilution.h <= 0.0))
 		throw Error(StatusCode::invalid_argument, "dilution parameters must be positive.");
 
+	if (!config.options.compile_options.enable_cuda && o.provider == Provider::cuda)
+		throw Error(StatusCode::unsupported, "CUDA provider requested, but CUDA is disabled in compile options.");
 	SimulationResult r;
+	r.kernel = detail::kernel_spec(config);
 	r.mode = config.mode;
 	r.total_states = atoms >= 31 ? 0 : (1 << atoms);
 	detail::ProgressTracker progress(config, r.rank, r.total_states, total_start);
@@ -752,6 +873,7 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 						st.expected_stages,
 						st.expected_tests};
 	r.provider = Provider::cuda;
+	r.kernel.provider = Provider::cuda;
 	r.evaluated_states = r.total_states;
 	r.evaluated_prior_mass = 1.0;
 	progress.replace_state(r.evaluated_states, r.evaluated_prior_mass, r.stats);
@@ -762,5 +884,72 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 	r.report_path = write_report_if_requested(config, r);
 	return r;
 }
+
+// bgt::CudaProvider (include/bgt/runtime.hpp:50-56): one tree simulation
+// through bgt_cuda_provider_run (CudaProvider::run, src/runtime/providers.cpp:73-133).
+class CudaProvider
+{
+  public:
+	bool available() const { return cuda_available(); }
+	TreeStats run(LatticeType type, int subjects, int variants, std::span<const host_probability_t> prior,
+				  const SimulationOptions &options, const DilutionTable *dilution) const
+	{
+		if (prior.size() != static_cast<std::size_t>(subjects) * static_cast<std::size_t>(variants))
+			throw Error(StatusCode::invalid_argument, "prior length must equal subjects * variants.");
+		const bool dil = detail::uses_dilution(type);
+		if (dil && dilution == nullptr)
+			throw Error(StatusCode::invalid_argument, "dilution table is required for dilution models.");
+		bgt_tree_stats st{};
+		detail::check(bgt_cuda_provider_run(dil ? 1 : 0, subjects, variants, prior.data(), options.search_depth,
+											options.threshold_up, options.threshold_lo, options.branch_threshold,
+											static_cast<int>(options.selector),
+											dil ? const_cast<host_probability_t **>(dilution->rows()) : nullptr,
+											&st));
+		return TreeStats{st.total_leaves,
+						 st.correct_probability,
+						 st.incorrect_probability,
+						 st.false_positive_probability,
+						 st.false_negative_probability,
+						 st.unclassified_probability,
+						 st.expected_stages,
+						 st.expected_tests};
+	}
+};
+
+// The CPU provider is always available, as in the reference; this package
+// runs only the device path.
+inline std::vector<Provider> available_providers()
+{
+	std::vector<Provider> out{Provider::cpu};
+	if (cuda_available())
+		out.push_back(Provider::cuda);
+	return out;
+}
+
+// bgt::Runtime (include/bgt/runtime.hpp:58-74) without run-time compilation:
+// the kernels are built ahead of time for sm_103a, so the JIT cache is empty.
+class Runtime
+{
+  public:
+	Runtime() = default;
+	explicit Runtime(std::filesystem::path cache_directory) : cache_directory_(std::move(cache_directory)) {}
+
+	std::vector<Provider> available_providers() const { return bgt::available_providers(); }
+	JitCacheInfo jit_cache_info() const
+	{
+		JitCacheInfo info;
+		info.disk_cache_directory = cache_directory_.string();
+		return info;
+	}
+	void clear_jit_cache() {}
+	KernelSpec make_kernel_spec(const SimulationConfig &config) const { return detail::kernel_spec(config); }
+	SimulationResult run_simulation(const SimulationConfig &config) { return bgt::run_simulation(config); }
+
+  private:
+	std::filesystem::path cache_directory_;
+};
+
+inline JitCacheInfo jit_cache_info() { return Runtime{}.jit_cache_info(); }
+inline void clear_jit_cache() {}
 
 } // namespace bgt

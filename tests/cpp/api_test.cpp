@@ -221,6 +221,32 @@ int main(int argc, char **argv)
 	expect_field(read_report(cancelled.report_path), "termination_reason", "cancellation_requested");
 	cfg.mode = bgt::SimulationMode::parallel_global_tree;
 	expect_error([&] { bgt::run_simulation(cfg); }, bgt::StatusCode::unsupported, "parallel mode");
+	cfg.mode = bgt::SimulationMode::local_tree;
+	cfg.report.write_csv = false;
+	cfg.progress.enabled = false;
+
+	// Runtime, KernelSpec and CudaProvider (include/bgt/runtime.hpp:50-74).
+	bgt::Runtime runtime;
+	const auto providers = runtime.available_providers();
+	expect_equal(providers.size() == 2 && providers[1] == bgt::Provider::cuda, 1, "providers cpu, cuda");
+	expect_equal(runtime.jit_cache_info().jit_enabled, 0, "no run-time compilation");
+	bgt::SimulationConfig dcfg = cfg;
+	dcfg.lattice_type = bgt::LatticeType::replicated_dilution;
+	dcfg.variants = 1;
+	const bgt::KernelSpec spec = runtime.make_kernel_spec(dcfg);
+	expect_equal(spec.dilution == bgt::DilutionMode::dilution, 1, "spec dilution");
+	expect_equal(spec.selector == bgt::SelectorType::op_bha, 1, "auto resolves to Op-BHA for k = 1");
+	expect_equal(bgt::KernelSpecHash{}(spec) == bgt::KernelSpecHash{}(runtime.make_kernel_spec(dcfg)), 1, "spec hash");
+	const bgt::SimulationResult rr = runtime.run_simulation(cfg);
+	expect_equal(rr.kernel.provider == bgt::Provider::cuda, 1, "result kernel provider");
+	expect_near(rr.stats.correct_probability, 0.792, 1e-12, "runtime run correct");
+	const std::vector<double> single{0.2};
+	const bgt::TreeStats ps = bgt::CudaProvider{}.run(bgt::LatticeType::replicated_non_dilution, 1, 1, single,
+													  cfg.options, nullptr);
+	expect_equal(ps.total_leaves, 2, "provider leaves");
+	expect_near(ps.unclassified_probability, 0.206, 1e-12, "provider unclassified");
+	cfg.options.compile_options.enable_cuda = false;
+	expect_error([&] { bgt::run_simulation(cfg); }, bgt::StatusCode::unsupported, "CUDA disabled in compile options");
 
 	std::printf("%s (%d failures)\n", failures ? "FAIL" : "ok", failures);
 	return failures ? 1 : 0;

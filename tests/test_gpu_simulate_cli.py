@@ -82,3 +82,16 @@ def test_progress_files(gpu, tmp_path):
     hist = [json.loads(x) for x in open(tmp_path / "run.progress.jsonl").read().splitlines()]
     assert [h["status"] for h in hist] == ["running", "completed"]
     assert hist[0]["message"] == "starting CUDA evaluation"
+
+
+def test_runtime_and_cuda_provider(gpu):
+    import bayesiangrouptesting_gb300 as bgt
+    cfg = bgt.SimulationConfig(subjects=1, prior=[0.2], options=bgt.SimulationOptions(provider=bgt.Provider.cuda))
+    res = bgt.Runtime().run_simulation(cfg)
+    assert res.kernel.provider == bgt.Provider.cuda and res.kernel.selector == bgt.SelectorType.op_bha
+    np.testing.assert_allclose(res.stats.as_array(), [2, 0.792, 0.002, 0.0, 0.002, 0.206, 1.0, 1.0], atol=1e-12)
+    st = bgt.CudaProvider().run(bgt.LatticeType.replicated_dilution, 2, 1, [0.2, 0.4], bgt.SimulationOptions(),
+                                bgt.DilutionTable(2, 0.99, 0.005))
+    want = bgt.run_simulation(bgt.SimulationConfig(lattice_type=bgt.LatticeType.replicated_dilution, subjects=2,
+                                                   prior=[0.2, 0.4])).stats
+    np.testing.assert_allclose(st.as_array(), want.as_array(), atol=0)

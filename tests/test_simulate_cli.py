@@ -101,3 +101,23 @@ def test_cancelled_before_evaluation(tmp_path):
     assert snap["status"] == "interrupted" and snap["message"] == "cancelled before evaluation started"
     hist = open(os.path.join(str(tmp_path), "cancelled.progress.jsonl")).read().splitlines()
     assert len(hist) == 1
+
+
+def test_runtime_and_kernel_spec():
+    # bgt::Runtime / KernelSpec (include/bgt/runtime.hpp:58-74): specs record
+    # the request; no run-time compilation; CUDA disabled in the compile
+    # options refuses Provider.cuda (src/runtime/simulation_runner.cpp:205-206).
+    rt = bgt.Runtime("cache")
+    cfg = bgt.SimulationConfig(subjects=3, variants=2, prior=[0.1] * 6,
+                               lattice_type=bgt.LatticeType.replicated_dilution)
+    spec = rt.make_kernel_spec(cfg)
+    assert spec.dilution == bgt.DilutionMode.dilution and spec.selector == bgt.SelectorType.op_bbpa
+    assert (spec.subjects, spec.variants, spec.cuda_arch) == (3, 2, "sm_103a")
+    info = rt.jit_cache_info()
+    assert not info.jit_enabled and info.memory_entries == 0 and info.disk_cache_directory == "cache"
+    rt.clear_jit_cache()
+    assert bgt.Provider.cpu in rt.available_providers()
+    cfg.options.provider = bgt.Provider.cuda
+    cfg.options.compile_options.enable_cuda = False
+    with pytest.raises(bgt.Error):
+        rt.run_simulation(cfg)
