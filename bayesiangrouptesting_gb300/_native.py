@@ -112,6 +112,7 @@ SIGNATURES = {
     "bgt_gpu_server_session_bytes": ([c_void_p, c_int, POINTER(c_uint64)], c_int),
     "bgt_gpu_lattice_reset": ([c_void_p, _dp], c_int),
     "bgt_gpu_selftest_bounded_wait": ([c_uint32, POINTER(c_int)], c_int),
+    "bgt_gpu_lattice_response_probability": ([c_void_p, c_uint32, c_uint32, c_uint32, POINTER(_dp), _dp], c_int),
     "bgt_gpu_profile_enable": ([c_int], c_int),
     "bgt_gpu_profile_read": ([POINTER(c_uint64), _dp], c_int),
     "bgt_gpu_select_noalloc": ([c_void_p, c_int, c_int, c_void_p, c_void_p], c_int),

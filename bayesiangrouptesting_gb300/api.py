@@ -626,6 +626,19 @@ class Lattice:
         _call(self._lib.bgt_gpu_lattice_upset_mass(self._handle, self._to_internal(experiment), ctypes.byref(out)))
         return out.value
 
+    def response_probability(self, experiment: int, response: int, true_state: int,
+                             dilution: Optional[DilutionTable] = None) -> float:
+        """P(response | experiment, true_state) under this lattice's likelihood
+        model (Lattice::response_probability, src/core/lattice_api.cpp:101-106);
+        public bit order."""
+        if _uses_dilution(self._type) and dilution is None:
+            raise ValueError("dilution table is required for dilution models.")
+        rows = dilution.rows() if dilution is not None else None
+        out = ctypes.c_double()
+        _call(self._lib.bgt_gpu_lattice_response_probability(self._handle, self._to_internal(experiment), response,
+                                                             self._to_internal(true_state), rows, ctypes.byref(out)))
+        return out.value
+
     def posterior(self) -> np.ndarray:
         """The whole normalised posterior in internal state order."""
         out = np.empty(1 << (self._subjects * self._variants))

@@ -1001,6 +1001,46 @@ int bgt_gpu_lattice_max_abs_diff(bgt_gpu_lattice *a, bgt_gpu_lattice *b, double 
 	});
 }
 
+int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
+										 uint32_t true_state, double **dilution, double *out)
+{
+	if (!lattice || !out)
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (lattice->dilution && !dilution)
+	{
+		set_error("dilution table is required for dilution models");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	// The likelihood model of the update kernels (ReplicatedNonDilutionLattice /
+	// ReplicatedDilutionLattice::response_prob, src/core/model/replicated_lattice.cpp:8-28),
+	// one factor per variant; internal bit order.
+	const int n = lattice->g.n, k = lattice->g.k;
+	const int pool = __builtin_popcount(experiment);
+	double p = 1.0;
+	for (int v = 0; v < k; v++)
+	{
+		const unsigned int sv = static_cast<unsigned int>(static_cast<uint64_t>(true_state) >> (v * n));
+		const bool positive_bit = ((response >> v) & 1u) != 0;
+		if (!lattice->dilution)
+		{
+			const bool contained = (experiment & sv) == experiment;
+			const double neg = BGT_NON_DILUTION_NEGATIVE;
+			p *= contained ? (positive_bit ? neg : 1.0 - neg) : (positive_bit ? 1.0 - neg : neg);
+		}
+		else
+		{
+			const int col = pool - __builtin_popcount(experiment & sv);
+			const double d = pool == 0 ? dilution[0][0] : dilution[pool - 1][col];
+			p *= positive_bit ? d : 1.0 - d;
+		}
+	}
+	*out = p;
+	return BGT_GPU_OK;
+}
+
 int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, double *out)
 {
 	if (!lattice || !out)

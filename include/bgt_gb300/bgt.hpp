@@ -281,6 +281,15 @@ class Lattice
 		detail::check(bgt_gpu_lattice_upset_mass(h_, to_internal(experiment), &out));
 		return out;
 	}
+	host_probability_t response_probability(state_t experiment, state_t response, state_t true_state,
+										  const DilutionTable *dilution = nullptr) const
+	{
+		double out = 0.0;
+		detail::check(bgt_gpu_lattice_response_probability(
+			h_, to_internal(experiment), response, to_internal(true_state),
+			dilution ? const_cast<host_probability_t **>(dilution->rows()) : nullptr, &out));
+		return out;
+	}
 	state_t select_experiment(SelectorType selector = SelectorType::auto_select) const
 	{
 		uint32_t e = 0;

@@ -146,6 +146,14 @@ BGT_GPU_API int bgt_gpu_lattice_read_posterior(bgt_gpu_lattice *lattice, double 
 BGT_GPU_API int bgt_gpu_lattice_posterior_probability(bgt_gpu_lattice *lattice, uint32_t state, double *out);
 BGT_GPU_API int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, double *out);
 
+/* Lattice::response_probability (include/bgt/lattice.hpp:52;
+ * src/core/lattice_api.cpp:101-106): P(response | experiment, true_state)
+ * under the lattice's likelihood model -- the factors its updates apply --
+ * in internal bit order; `dilution` as for update, required for dilution
+ * lattices (status 1 without it). */
+BGT_GPU_API int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
+													 uint32_t true_state, double **dilution, double *out);
+
 /* max over states of |p_a(s) - p_b(s)| between the normalised posteriors of
  * two lattices of the same shape, computed on the device (the FP32-vs-FP64
  * error report; 2^30-state lattices need no host copy).  No reference

@@ -141,6 +141,9 @@ int main(int argc, char **argv)
 	expect_near(lattice.upset_probability_mass(1), 0.60, 1e-12, "upset mass 1");
 	expect_near(lattice.upset_probability_mass(2), 0.80, 1e-12, "upset mass 2");
 	expect_near(lattice.upset_probability_mass(3), 0.48, 1e-12, "upset mass 3");
+	expect_near(lattice.response_probability(1, 1, 3), 0.99, 1e-15, "response probability, contained");
+	expect_near(lattice.response_probability(1, 1, 2), 0.01, 1e-15, "response probability, not contained");
+	expect_near(lattice.response_probability(3, 0, 1), 0.99, 1e-15, "response probability, positive");
 	expect_equal(lattice.select_experiment(), 3, "auto selection");
 	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bha), 3, "Op-BHA selection");
 	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bbpa), 3, "Op-BBPA selection");

@@ -159,3 +159,24 @@ def test_multinomial_update_masses(gpu, oracle):
         assert_posterior_close(lat.posterior(), post, step + 1)
         np.testing.assert_allclose(lat.atom_masses(), oracle.atom_masses(post, n * k), rtol=1e-12, atol=1e-18)
         assert lat.select_experiment() == oracle.select(post, n, k, 0)
+
+
+@pytest.mark.parametrize("n,k,dilution", [(5, 1, False), (5, 1, True), (3, 2, False), (4, 3, True)])
+def test_response_probability_matches_oracle(gpu, oracle, n, k, dilution):
+    # Lattice::response_probability (src/core/lattice_api.cpp:101-106): the
+    # public order is bit-reversed for k = 1, the oracle takes internal order.
+    rng = np.random.default_rng(40 + n + k)
+    t = bgt.LatticeType.replicated_dilution if dilution else bgt.LatticeType.replicated_non_dilution
+    lat = bgt.Lattice(t, n, rng.uniform(0.02, 0.3, n * k), k)
+    table = bgt.api.DilutionTable(n, 0.99, 0.005) if dilution else None
+    rev = (lambda v: bgt.reverse_bits(v, n)) if k == 1 else (lambda v: v)
+    for _ in range(200):
+        e = int(rng.integers(1, 1 << n))
+        r = int(rng.integers(0, 1 << k))
+        s = int(rng.integers(0, 1 << (n * k)))
+        got = lat.response_probability(e, r, s, table)
+        want = oracle.response_prob(int(dilution), n, k, rev(e), r, rev(s), 0.99, 0.005)
+        assert abs(got - want) <= 1e-15, (e, r, s, got, want)
+    if dilution:
+        with pytest.raises(ValueError):
+            lat.response_probability(1, 1, 0)
