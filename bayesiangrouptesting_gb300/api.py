@@ -332,6 +332,23 @@ class SimulationTimings:
 
 
 @dataclass
+class TestAccuracy:
+    """Non-dilution test accuracy, an extension: the reference fixes both at
+    0.99 (src/core/model/replicated_lattice.cpp:6-14).  P(negative response |
+    no pooled positive) = specificity, P(positive response | a pooled
+    positive) = sensitivity, per variant."""
+
+    __test__ = False  # not a pytest class
+
+    sensitivity: float = 0.99
+    specificity: float = 0.99
+
+    def validate(self) -> None:
+        if not (0.0 <= self.sensitivity <= 1.0 and 0.0 <= self.specificity <= 1.0):
+            raise ValueError("sensitivity and specificity must lie in [0, 1].")
+
+
+@dataclass
 class SimulationConfig:
     """bgt::SimulationConfig (include/bgt/simulation.hpp:87-103).  As on the
     reference's CUDA path, evaluation_prior, true_state_policy, trim_percent,
@@ -352,6 +369,8 @@ class SimulationConfig:
     dilution: DilutionParameters = field(default_factory=DilutionParameters)
     report: ReportConfig = field(default_factory=ReportConfig)
     progress: ProgressConfig = field(default_factory=ProgressConfig)
+    # Extension: a non-dilution likelihood other than the reference's 0.99 / 0.99.
+    test_accuracy: Optional[TestAccuracy] = None
 
 
 @dataclass
@@ -466,7 +485,8 @@ class CudaProvider:
         return cuda_available()
 
     def run(self, type: LatticeType, subjects: int, variants: int, prior, options: SimulationOptions,
-            dilution: "Optional[DilutionTable]" = None) -> TreeStats:
+            dilution: "Optional[DilutionTable]" = None,
+            test_accuracy: Optional[TestAccuracy] = None) -> TreeStats:
         prior = np.ascontiguousarray(prior, dtype=np.float64)
         if prior.size != subjects * variants:
             raise ValueError("prior length must equal subjects * variants.")
@@ -474,6 +494,16 @@ class CudaProvider:
         if dil and dilution is None:
             raise ValueError("dilution table is required for dilution models.")
         stats = TreeStatsC()
+        if test_accuracy is not None:
+            if dil:
+                raise ValueError("test accuracy applies to non-dilution models.")
+            test_accuracy.validate()
+            _call(load().bgt_gpu_tree_run_accuracy(subjects, variants, prior.ctypes.data_as(_dp), options.search_depth,
+                                                   options.threshold_up, options.threshold_lo,
+                                                   options.branch_threshold, int(options.selector),
+                                                   test_accuracy.sensitivity, test_accuracy.specificity,
+                                                   ctypes.byref(stats)))
+            return TreeStats.from_c(stats)
         _call(load().bgt_cuda_provider_run(1 if dil else 0, subjects, variants, prior.ctypes.data_as(_dp),
                                            options.search_depth, options.threshold_up, options.threshold_lo,
                                            options.branch_threshold, int(options.selector),
@@ -501,6 +531,10 @@ def _validate(config: SimulationConfig) -> None:
     if config.mode == SimulationMode.local_tree and config.lattice_type in (LatticeType.distributed_non_dilution,
                                                                              LatticeType.distributed_dilution):
         raise ValueError("local_tree requires a replicated lattice.")
+    if config.test_accuracy is not None:
+        if _uses_dilution(config.lattice_type):
+            raise ValueError("test accuracy applies to non-dilution models.")
+        config.test_accuracy.validate()
     if config.mode != SimulationMode.local_tree:
         raise Error(StatusCode.unsupported, "parallel simulation modes need the MPI backend; "
                     "the GB300 provider serves local_tree on one GPU.")
@@ -542,11 +576,19 @@ def run_simulation(config: SimulationConfig) -> SimulationResult:
     if _uses_dilution(config.lattice_type):
         dil = DilutionTable(config.subjects, config.dilution.alpha, config.dilution.h)
     stats = TreeStatsC()
-    status = lib.bgt_cuda_provider_run(1 if dil else 0, config.subjects, config.variants, prior.ctypes.data_as(_dp),
-                                       config.options.search_depth, config.options.threshold_up,
-                                       config.options.threshold_lo, config.options.branch_threshold,
-                                       int(_resolve_selector(config.options.selector, config.variants)),
-                                       dil.rows() if dil else None, ctypes.byref(stats))
+    selector = int(_resolve_selector(config.options.selector, config.variants))
+    if config.test_accuracy is not None:
+        status = lib.bgt_gpu_tree_run_accuracy(config.subjects, config.variants, prior.ctypes.data_as(_dp),
+                                               config.options.search_depth, config.options.threshold_up,
+                                               config.options.threshold_lo, config.options.branch_threshold, selector,
+                                               config.test_accuracy.sensitivity, config.test_accuracy.specificity,
+                                               ctypes.byref(stats))
+    else:
+        status = lib.bgt_cuda_provider_run(1 if dil else 0, config.subjects, config.variants,
+                                           prior.ctypes.data_as(_dp), config.options.search_depth,
+                                           config.options.threshold_up, config.options.threshold_lo,
+                                           config.options.branch_threshold, selector, dil.rows() if dil else None,
+                                           ctypes.byref(stats))
     _call(status)
     result.stats = TreeStats.from_c(stats)
     result.provider = Provider.cuda
@@ -625,6 +667,15 @@ class Lattice:
         out = ctypes.c_double()
         _call(self._lib.bgt_gpu_lattice_upset_mass(self._handle, self._to_internal(experiment), ctypes.byref(out)))
         return out.value
+
+    def set_test_accuracy(self, sensitivity: float, specificity: float) -> None:
+        """Non-dilution likelihood for later updates, sessions and
+        response_probability (an extension: the reference fixes both at 0.99);
+        bgt_gpu_lattice_set_test_accuracy."""
+        if _uses_dilution(self._type):
+            raise ValueError("test accuracy applies to non-dilution models.")
+        TestAccuracy(sensitivity, specificity).validate()
+        _call(self._lib.bgt_gpu_lattice_set_test_accuracy(self._handle, float(sensitivity), float(specificity)))
 
     def response_probability(self, experiment: int, response: int, true_state: int,
                              dilution: Optional[DilutionTable] = None) -> float:

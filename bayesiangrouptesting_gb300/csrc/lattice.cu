@@ -1027,8 +1027,8 @@ int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t expe
 		if (!lattice->dilution)
 		{
 			const bool contained = (experiment & sv) == experiment;
-			const double neg = BGT_NON_DILUTION_NEGATIVE;
-			p *= contained ? (positive_bit ? neg : 1.0 - neg) : (positive_bit ? 1.0 - neg : neg);
+			const double spec = specificity_of(lattice->host), sens = sensitivity_of(lattice->host);
+			p *= contained ? (positive_bit ? spec : 1.0 - spec) : (positive_bit ? 1.0 - sens : sens);
 		}
 		else
 		{
@@ -1039,6 +1039,34 @@ int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t expe
 	}
 	*out = p;
 	return BGT_GPU_OK;
+}
+
+int bgt_gpu_lattice_set_test_accuracy(bgt_gpu_lattice *lattice, double sensitivity, double specificity)
+{
+	if (!lattice)
+	{
+		set_error("null lattice");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (lattice->dilution)
+	{
+		set_error("test accuracy applies to non-dilution lattices; dilution lattices use their DilutionTable");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (!valid_accuracy(sensitivity, specificity))
+	{
+		set_error("sensitivity and specificity must lie in [0, 1]");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return guarded([&]() -> int {
+		if (lattice->update_pending)
+			lattice->run_k1(); // a pending update keeps the accuracy it was made under
+		apply_accuracy(lattice->host, TestAccuracy{1, specificity, sensitivity});
+		lattice->set_field(offsetof(LatticeDev, accuracy_set), 1);
+		lattice->set_field(offsetof(LatticeDev, spec), specificity);
+		lattice->set_field(offsetof(LatticeDev, sens), sensitivity);
+		return BGT_GPU_OK;
+	});
 }
 
 int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t experiment, double *out)

@@ -776,7 +776,8 @@ __device__ __forceinline__ void load_class_table(const LatticeDev &L, unsigned i
 			rest /= radix;
 			// Non-dilution class c = contained (1) or not (0); dilution class = popcount(e & s_v).
 			const int pc = L.dilution ? c : (c ? pool : (pool > 0 ? pool - 1 : 0));
-			f *= binary_likelihood(L.dilution, pool, pc, (L.pend_r >> v) & 1u, L.dil, L.orig_n + 1);
+			f *= binary_likelihood(L.dilution, pool, pc, (L.pend_r >> v) & 1u, L.dil, L.orig_n + 1, specificity_of(L),
+								   sensitivity_of(L));
 		}
 		if (L.fp32)
 			reinterpret_cast<float *>(g_ctab)[idx] = static_cast<float>(f / z);
@@ -800,7 +801,9 @@ __device__ __forceinline__ void fill_lattice_cache(const LatticeDev &L, int li, 
 		if (with_ctab && mode == kUpdate && k == 1)
 		{
 			ps.ctab[tid] = static_cast<int>(tid) <= pool
-							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1) / L.z_norm
+							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1,
+												   specificity_of(L), sensitivity_of(L)) /
+									 L.z_norm
 							   : 0.0;
 			ps.ctab32[tid] = static_cast<float>(ps.ctab[tid]);
 		}
@@ -1500,8 +1503,9 @@ __device__ void k2_epilogue(LatticeDev &L, unsigned int per)
 			const bool settled = L.sess_stop && st > 0 && (L.pos | L.neg) == all_atoms;
 			if (st < L.stages && !settled)
 			{
-				const unsigned int rsp = bgt_session_sample_response(L.dilution, L.n, L.k, be, L.truth, L.alpha, L.hpar,
-																	 L.seed, L.session, static_cast<uint32_t>(st));
+				const unsigned int rsp = bgt_session_sample_response(
+					L.dilution, L.n, L.k, be, L.truth, L.alpha, L.hpar, specificity_of(L), sensitivity_of(L), L.seed,
+					L.session, static_cast<uint32_t>(st));
 				if (L.out_e)
 					L.out_e[st] = be;
 				if (L.out_r)

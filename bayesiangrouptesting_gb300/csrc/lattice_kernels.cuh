@@ -115,6 +115,11 @@ struct LatticeDev
 	int dilution; // 0 / 1
 	int orig_n;   // subjects of the dilution table
 	int fp32;     // posterior stored as FP32 (q_in / q_out then point to floats)
+	// Non-dilution test accuracy: 0 = the reference's fixed model (both
+	// BGT_NON_DILUTION_NEGATIVE), else spec / sens below.
+	int accuracy_set;
+	double spec;  // P(negative response | no pooled positive)
+	double sens;  // P(positive response | a pooled positive)
 	// ---- buffers (host-set) ----
 	const double *q_in;
 	double *q_out;
@@ -363,19 +368,52 @@ __device__ __host__ __forceinline__ double pow2_neg(int s)
 #endif
 }
 
+// A non-dilution test accuracy as the host passes it around; `set` = 0 is
+// the reference's fixed model.
+struct TestAccuracy
+{
+	int set;
+	double spec, sens;
+};
+
+constexpr TestAccuracy kReferenceAccuracy{0, BGT_NON_DILUTION_NEGATIVE, BGT_NON_DILUTION_NEGATIVE};
+
+inline bool valid_accuracy(double sensitivity, double specificity)
+{
+	return sensitivity >= 0.0 && sensitivity <= 1.0 && specificity >= 0.0 && specificity <= 1.0;
+}
+
+inline void apply_accuracy(LatticeDev &L, const TestAccuracy &a)
+{
+	L.accuracy_set = a.set;
+	L.spec = a.spec;
+	L.sens = a.sens;
+}
+
+__host__ __device__ __forceinline__ double specificity_of(const LatticeDev &L)
+{
+	return L.accuracy_set ? L.spec : BGT_NON_DILUTION_NEGATIVE;
+}
+
+__host__ __device__ __forceinline__ double sensitivity_of(const LatticeDev &L)
+{
+	return L.accuracy_set ? L.sens : BGT_NON_DILUTION_NEGATIVE;
+}
+
 // Likelihood of response r for a binary lattice at pool class pc =
 // popcount(e & s) (negatives in the pool), restating
 // ReplicatedNonDilutionLattice / ReplicatedDilutionLattice::response_prob
-// (src/core/model/replicated_lattice.cpp:8-28) for one variant.
+// (src/core/model/replicated_lattice.cpp:8-28) for one variant.  The
+// non-dilution factors are the reference's with its fixed 0.99 split into
+// specificity (pool contained) and sensitivity (not contained); both at
+// BGT_NON_DILUTION_NEGATIVE give the reference's values bit for bit.
 __device__ __forceinline__ double binary_likelihood(int dilution, int pool, int pc, unsigned int r, const double *dil,
-												   int dil_stride)
+												   int dil_stride, double spec, double sens)
 {
 	if (!dilution)
 	{
-		const double negative_response = BGT_NON_DILUTION_NEGATIVE;
 		const bool contained = pc == pool;
-		return contained ? ((r & 1u) == 0 ? (1.0 - negative_response) : negative_response)
-						 : ((r & 1u) == 0 ? negative_response : (1.0 - negative_response));
+		return contained ? ((r & 1u) == 0 ? (1.0 - spec) : spec) : ((r & 1u) == 0 ? sens : (1.0 - sens));
 	}
 	const int col = pool - pc;
 	const double p = pool == 0 ? dil[0] : dil[(pool - 1) * dil_stride + col];

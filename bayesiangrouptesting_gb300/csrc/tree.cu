@@ -60,11 +60,12 @@ struct SweepParams
 {
 	int atoms, subjects, variants, dilution, count;
 	const int *count_dev; // when set, the node count lives in device memory
-	const double *thres_dev; // when set, the branch threshold lives in device memory
+	const double *thres_dev; // when set, {branch threshold, spec, sens} live in device memory
 	double thres;
 	int leaf_sums; // the node list's leaves carry their contributions: nothing to do at threshold <= 0
 	const double *pi0;
 	const double *dil; // [subjects][subjects + 1]
+	double spec, sens; // non-dilution test accuracy (the reference's: both BGT_NON_DILUTION_NEGATIVE)
 	const SweepNode *nodes;
 	double *partials;  // [gridDim.x][7]
 };
@@ -79,7 +80,7 @@ __device__ __forceinline__ double edge_factor(const SweepParams &p, unsigned int
 	{
 		const unsigned int shifted = static_cast<unsigned int>(static_cast<unsigned long long>(t) >> (v * p.subjects));
 		const int pc = __popc(e & shifted);
-		ret *= binary_likelihood(p.dilution, pool, pc, (r >> v) & 1u, p.dil, p.subjects + 1);
+		ret *= binary_likelihood(p.dilution, pool, pc, (r >> v) & 1u, p.dil, p.subjects + 1, p.spec, p.sens);
 	}
 	return ret;
 }
@@ -93,7 +94,11 @@ __global__ void __launch_bounds__(kSweepThreads) tree_sweep(SweepParams p)
 	if (p.count_dev)
 		p.count = *p.count_dev;
 	if (p.thres_dev)
-		p.thres = *p.thres_dev;
+	{
+		p.thres = p.thres_dev[0];
+		p.spec = p.thres_dev[1];
+		p.sens = p.thres_dev[2];
+	}
 	if (p.leaf_sums && p.thres <= 0.0)
 		return;
 	double acc[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -653,7 +658,7 @@ void build_tree_graph(TreeGraph &t)
 	t.d_dil = t.dev<double>(static_cast<size_t>(g.n) * (g.n + 1), "alloc dilution");
 	t.d_lo = t.dev<double>(size_t{1} << g.tbits, "alloc prior lo");
 	t.d_hi = t.dev<double>(rows, "alloc prior hi");
-	t.d_thres = t.dev<double>(1, "alloc threshold");
+	t.d_thres = t.dev<double>(3, "alloc threshold");
 	int sms = sm_count();
 	const unsigned long long total = 1ull << g.atoms;
 	t.sweep_blocks = static_cast<int>(
@@ -663,7 +668,7 @@ void build_tree_graph(TreeGraph &t)
 	cuda_check(cudaHostAlloc(&t.h_dil, std::max<size_t>(1, static_cast<size_t>(g.n) * (g.n + 1)) * sizeof(double),
 							 cudaHostAllocDefault),
 			   "pinned dilution");
-	cuda_check(cudaHostAlloc(&t.h_thres, sizeof(double), cudaHostAllocDefault), "pinned threshold");
+	cuda_check(cudaHostAlloc(&t.h_thres, 3 * sizeof(double), cudaHostAllocDefault), "pinned threshold");
 	cuda_check(cudaHostAlloc(&t.h_partials, static_cast<size_t>(t.sweep_blocks) * 7 * sizeof(double),
 							 cudaHostAllocDefault),
 			   "pinned partials");
@@ -755,7 +760,7 @@ uint64_t enqueue_tree(TreeGraph &t)
 		cuda_check(cudaMemcpyAsync(t.d_dil, t.h_dil, static_cast<size_t>(g.n) * (g.n + 1) * sizeof(double),
 								   cudaMemcpyHostToDevice, s),
 				   "dilution up");
-	cuda_check(cudaMemcpyAsync(t.d_thres, t.h_thres, sizeof(double), cudaMemcpyHostToDevice, s), "threshold up");
+	cuda_check(cudaMemcpyAsync(t.d_thres, t.h_thres, 3 * sizeof(double), cudaMemcpyHostToDevice, s), "threshold up");
 	cuda_check(cudaMemcpyAsync(t.states[0], t.h_root, sizeof(LatticeDev), cudaMemcpyHostToDevice, s), "root up");
 	cuda_check(cudaMemcpyAsync(t.recs, t.h_rootrec, sizeof(TreeNodeRec), cudaMemcpyHostToDevice, s),
 			   "root record up");
@@ -819,7 +824,8 @@ uint64_t enqueue_tree(TreeGraph &t)
 // The device-built tree: same results as the level loop below, one graph
 // launch per simulation.
 void run_tree_graph(int use_dilution, int subjects, int variants, const double *prior, int search_depth, double up,
-					double lo, double branch_threshold, const std::vector<double> &dil_flat, bgt_tree_stats *stats)
+					double lo, double branch_threshold, const std::vector<double> &dil_flat, const TestAccuracy &acc,
+					bgt_tree_stats *stats)
 {
 	TreeGraph *t = g_tree_graph.get();
 	if (!t || t->subjects != subjects || t->variants != variants || t->depth != search_depth ||
@@ -840,7 +846,10 @@ void run_tree_graph(int use_dilution, int subjects, int variants, const double *
 	std::memcpy(t->h_pi0, prior, g.atoms * sizeof(double));
 	if (use_dilution)
 		std::memcpy(t->h_dil, dil_flat.data(), dil_flat.size() * sizeof(double));
-	*t->h_thres = branch_threshold;
+	t->h_thres[0] = branch_threshold;
+	t->h_thres[1] = acc.spec;
+	t->h_thres[2] = acc.sens;
+	apply_accuracy(*t->h_root, acc);
 	t->h_root->up = up;
 	t->h_root->lo = lo;
 	if (profiling_enabled())
@@ -910,7 +919,8 @@ void run_tree_graph(int use_dilution, int subjects, int variants, const double *
 // Builds the tree and evaluates TreeStats; throws CudaFailure on error.
 // Returns a status when the request is unsupported.
 int run_tree(int use_dilution, int subjects, int variants, const double *prior, int search_depth, double up, double lo,
-			 double branch_threshold, int selector, const std::vector<double> &dil_flat, bgt_tree_stats *stats)
+			 double branch_threshold, int selector, const std::vector<double> &dil_flat, const TestAccuracy &acc,
+			 bgt_tree_stats *stats)
 {
 	const LatticeGeometry g = tuned_geometry(subjects, variants, 16);
 	configure_kernels();
@@ -984,6 +994,7 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 		d.up = up;
 		d.lo = lo;
 		d.classify_on_update = 1;
+		apply_accuracy(d, acc);
 		d.blk_list = lists.blocks;
 		d.cblk_list = lists.cblks;
 	}
@@ -1120,6 +1131,8 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 	sp.dilution = use_dilution;
 	sp.count = static_cast<int>(flat.size());
 	sp.thres = branch_threshold;
+	sp.spec = acc.spec;
+	sp.sens = acc.sens;
 	sp.pi0 = static_cast<double *>(d_pi0.ptr);
 	sp.dil = static_cast<double *>(d_dil.ptr);
 	sp.nodes = static_cast<SweepNode *>(d_nodes.ptr);
@@ -1151,11 +1164,12 @@ int run_tree(int use_dilution, int subjects, int variants, const double *prior, 
 
 using namespace bgt_gpu;
 
-extern "C" {
+namespace
+{
 
-int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const double *prior, int search_depth,
-						  double threshold_up, double threshold_lo, double branch_threshold, int selector,
-						  double **dilution, bgt_tree_stats *stats)
+int provider_run(int use_dilution, int subjects, int variants, const double *prior, int search_depth,
+				 double threshold_up, double threshold_lo, double branch_threshold, int selector, double **dilution,
+				 const TestAccuracy &acc, bgt_tree_stats *stats)
 {
 	if (stats == nullptr)
 	{
@@ -1218,17 +1232,44 @@ int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const do
 		if (tree_graph_fits(make_geometry(subjects, variants), variants, search_depth))
 		{
 			run_tree_graph(use_dilution, subjects, variants, prior, search_depth, threshold_up, threshold_lo,
-						   branch_threshold, flat, stats);
+						   branch_threshold, flat, acc, stats);
 			return BGT_GPU_OK;
 		}
 		return run_tree(use_dilution, subjects, variants, prior, search_depth, threshold_up, threshold_lo,
-						branch_threshold, resolved, flat, stats);
+						branch_threshold, resolved, flat, acc, stats);
 	}
 	catch (const std::exception &ex)
 	{
 		set_error(ex.what());
 		return BGT_GPU_RUNTIME_FAILURE;
 	}
+}
+
+} // namespace
+
+extern "C" {
+
+int bgt_cuda_provider_run(int use_dilution, int subjects, int variants, const double *prior, int search_depth,
+						  double threshold_up, double threshold_lo, double branch_threshold, int selector,
+						  double **dilution, bgt_tree_stats *stats)
+{
+	return provider_run(use_dilution, subjects, variants, prior, search_depth, threshold_up, threshold_lo,
+						branch_threshold, selector, dilution, kReferenceAccuracy, stats);
+}
+
+int bgt_gpu_tree_run_accuracy(int subjects, int variants, const double *prior, int search_depth, double threshold_up,
+							  double threshold_lo, double branch_threshold, int selector, double sensitivity,
+							  double specificity, bgt_tree_stats *stats)
+{
+	if (stats != nullptr)
+		*stats = bgt_tree_stats{};
+	if (!valid_accuracy(sensitivity, specificity))
+	{
+		set_error("sensitivity and specificity must lie in [0, 1]");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	return provider_run(0, subjects, variants, prior, search_depth, threshold_up, threshold_lo, branch_threshold,
+						selector, nullptr, TestAccuracy{1, specificity, sensitivity}, stats);
 }
 
 int bgt_cuda_provider_benchmark_select(int subjects, int variants, const double *prior, int selector, int iterations,

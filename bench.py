@@ -82,7 +82,7 @@ def session_response(dilution: bool, n: int, e: int, s: int, alpha: float, h: fl
     """Host copy of bgt_session_sample_response for one binary variant
     (include/bgt_session_rng.h): bit 0 set = the pool tested negative."""
     if not dilution:
-        p1 = 0.99 if (e & s) == e else 0.01
+        p1 = 0.99 if (e & s) == e else 1.0 - 0.99
     else:
         pool = bin(e).count("1")
         pos = pool - bin(e & s).count("1")

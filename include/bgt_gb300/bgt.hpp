@@ -281,6 +281,12 @@ class Lattice
 		detail::check(bgt_gpu_lattice_upset_mass(h_, to_internal(experiment), &out));
 		return out;
 	}
+	// Extension: the non-dilution likelihood of later updates
+	// (bgt_gpu_lattice_set_test_accuracy).
+	void set_test_accuracy(host_probability_t sensitivity, host_probability_t specificity)
+	{
+		detail::check(bgt_gpu_lattice_set_test_accuracy(h_, sensitivity, specificity));
+	}
 	host_probability_t response_probability(state_t experiment, state_t response, state_t true_state,
 										  const DilutionTable *dilution = nullptr) const
 	{
@@ -418,6 +424,16 @@ struct ProgressConfig
 // reference's CUDA path, evaluation_prior, true_state_policy, trim_percent,
 // global_tree_depth and workload_granularity do not change a local_tree run on
 // the device (every true state is evaluated under the prior).
+// Non-dilution test accuracy, an extension: the reference fixes both at 0.99
+// (src/core/model/replicated_lattice.cpp:6-14).  P(negative response | no
+// pooled positive) = specificity, P(positive response | a pooled positive) =
+// sensitivity, per variant.
+struct TestAccuracy
+{
+	host_probability_t sensitivity = 0.99;
+	host_probability_t specificity = 0.99;
+};
+
 struct SimulationConfig
 {
 	LatticeType lattice_type = LatticeType::replicated_non_dilution;
@@ -434,6 +450,7 @@ struct SimulationConfig
 	DilutionParameters dilution;
 	ReportConfig report;
 	ProgressConfig progress;
+	std::optional<TestAccuracy> test_accuracy; // extension; unset = the reference's model
 };
 
 // bgt::KernelSpec (include/bgt/types.hpp:132-181): what a run asks for.
@@ -844,6 +861,8 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 	const bool dil = detail::uses_dilution(config.lattice_type);
 	if (dil && (config.dilution.alpha <= 0.0 || config.dilution.h <= 0.0))
 		throw Error(StatusCode::invalid_argument, "dilution parameters must be positive.");
+	if (config.test_accuracy && dil)
+		throw Error(StatusCode::invalid_argument, "test accuracy applies to non-dilution models.");
 
 	if (!config.options.compile_options.enable_cuda && o.provider == Provider::cuda)
 		throw Error(StatusCode::unsupported, "CUDA provider requested, but CUDA is disabled in compile options.");
@@ -870,9 +889,15 @@ inline SimulationResult run_simulation(const SimulationConfig &config)
 	if (dil)
 		table = DilutionTable(config.subjects, config.dilution.alpha, config.dilution.h);
 	bgt_tree_stats st{};
-	detail::check(bgt_cuda_provider_run(dil ? 1 : 0, config.subjects, config.variants, config.prior.data(),
-										o.search_depth, o.threshold_up, o.threshold_lo, o.branch_threshold,
-										static_cast<int>(o.selector), dil ? table.rows() : nullptr, &st));
+	if (config.test_accuracy)
+		detail::check(bgt_gpu_tree_run_accuracy(config.subjects, config.variants, config.prior.data(), o.search_depth,
+												o.threshold_up, o.threshold_lo, o.branch_threshold,
+												static_cast<int>(o.selector), config.test_accuracy->sensitivity,
+												config.test_accuracy->specificity, &st));
+	else
+		detail::check(bgt_cuda_provider_run(dil ? 1 : 0, config.subjects, config.variants, config.prior.data(),
+											o.search_depth, o.threshold_up, o.threshold_lo, o.branch_threshold,
+											static_cast<int>(o.selector), dil ? table.rows() : nullptr, &st));
 	r.stats = TreeStats{st.total_leaves,
 						st.correct_probability,
 						st.incorrect_probability,

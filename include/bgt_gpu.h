@@ -86,6 +86,15 @@ BGT_GPU_API int bgt_cuda_provider_run(int use_dilution, int subjects, int varian
 									  double branch_threshold, int selector, double **dilution,
 									  bgt_tree_stats *stats);
 
+/* bgt_cuda_provider_run for a non-dilution lattice under the test accuracy
+ * of bgt_gpu_lattice_set_test_accuracy (tree updates, branch probabilities
+ * and the leaf sweep all use it); 0.99 / 0.99 equals bgt_cuda_provider_run
+ * with use_dilution = 0. */
+BGT_GPU_API int bgt_gpu_tree_run_accuracy(int subjects, int variants, const double *prior, int search_depth,
+										  double threshold_up, double threshold_lo, double branch_threshold,
+										  int selector, double sensitivity, double specificity,
+										  bgt_tree_stats *stats);
+
 /* Replaces bgt_cuda_provider_benchmark_select
  * (include/bgt/detail/cuda_provider.hpp:14-24, cuda_provider.cu:2449-2551):
  * builds the prior lattice, then times `iterations` selections after
@@ -153,6 +162,16 @@ BGT_GPU_API int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t ex
  * lattices (status 1 without it). */
 BGT_GPU_API int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
 													 uint32_t true_state, double **dilution, double *out);
+
+/* Non-dilution test accuracy (an extension: the reference fixes both at 0.99,
+ * src/core/model/replicated_lattice.cpp:6-14).  Later updates, sessions and
+ * response_probability use
+ *   P(negative response | no pooled positive)  = specificity,
+ *   P(positive response | a pooled positive)   = sensitivity
+ * for each variant; 0.99 / 0.99 reproduces the reference bit for bit.  A
+ * pending update is applied first, under the accuracy it was made with.
+ * Status 2 for a dilution lattice or a value outside [0, 1]. */
+BGT_GPU_API int bgt_gpu_lattice_set_test_accuracy(bgt_gpu_lattice *lattice, double sensitivity, double specificity);
 
 /* max over states of |p_a(s) - p_b(s)| between the normalised posteriors of
  * two lattices of the same shape, computed on the device (the FP32-vs-FP64

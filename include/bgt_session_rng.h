@@ -59,20 +59,19 @@ BGT_RNG_FN int bgt_popcount32(uint32_t v)
 }
 
 /* Probability that response bit `variant` is 1 (pool negative) for
- * experiment e (subject mask) and true state s.  Non-dilution: 0.99 when the
- * pool is "contained" (all pooled subjects negative for the variant), else
- * 0.01.  Dilution: the DilutionTable entry for pool size L and r positives in
- * the pool, alpha for r = 0 and 1 - alpha*r/((L-r)*h + r) otherwise; an empty
+ * experiment e (subject mask) and true state s.  Non-dilution: `specificity`
+ * when the pool is "contained" (all pooled subjects negative for the
+ * variant), else 1 - `sensitivity`; the reference's model is
+ * specificity = sensitivity = BGT_NON_DILUTION_NEGATIVE (0.99 and 0.01).
+ * Dilution: the DilutionTable entry for pool size L and r positives in the
+ * pool, alpha for r = 0 and 1 - alpha*r/((L-r)*h + r) otherwise; an empty
  * pool (L = 0) is given alpha, the r = 0 value. */
 BGT_RNG_FN double bgt_response_bit_probability(int dilution, int subjects, uint32_t e, uint32_t s, int variant,
-											   double alpha, double h)
+											   double alpha, double h, double specificity, double sensitivity)
 {
 	const uint32_t variant_state = (uint32_t)(((uint64_t)s) >> (variant * subjects));
 	if (!dilution)
-	{
-		const double negative = BGT_NON_DILUTION_NEGATIVE;
-		return (e & variant_state) == e ? negative : 1.0 - negative;
-	}
+		return (e & variant_state) == e ? specificity : 1.0 - sensitivity;
 	const int pool = bgt_popcount32(e);
 	const int positives = pool - bgt_popcount32(e & variant_state);
 	if (positives == 0)
@@ -83,13 +82,13 @@ BGT_RNG_FN double bgt_response_bit_probability(int dilution, int subjects, uint3
 
 /* Response word for one stage of one session. */
 BGT_RNG_FN uint32_t bgt_session_sample_response(int dilution, int subjects, int variants, uint32_t e, uint32_t s,
-												double alpha, double h, uint64_t seed, uint64_t session,
-												uint32_t stage)
+												double alpha, double h, double specificity, double sensitivity,
+												uint64_t seed, uint64_t session, uint32_t stage)
 {
 	uint32_t response = 0;
 	for (int v = 0; v < variants; v++)
 	{
-		const double p1 = bgt_response_bit_probability(dilution, subjects, e, s, v, alpha, h);
+		const double p1 = bgt_response_bit_probability(dilution, subjects, e, s, v, alpha, h, specificity, sensitivity);
 		const double u = bgt_uniform(seed, session, BGT_RNG_TAG_RESPONSE, stage * 64u + (uint32_t)v);
 		if (u < p1)
 			response |= 1u << v;

@@ -50,6 +50,20 @@ ORC_EXPORT void orc_dilution_table(int n, double alpha, double h, double *out)
 	}
 }
 
+/* Non-dilution test accuracy.  The reference fixes both at
+ * BGT_NON_DILUTION_NEGATIVE (src/core/model/replicated_lattice.cpp:6); other
+ * values restate the same formula with P(negative | contained) = specificity
+ * and P(positive | not contained) = sensitivity -- an extension the reference
+ * cannot express, so results at other values are unpinned. */
+static double g_specificity = BGT_NON_DILUTION_NEGATIVE;
+static double g_sensitivity = BGT_NON_DILUTION_NEGATIVE;
+
+ORC_EXPORT void orc_set_test_accuracy(double sensitivity, double specificity)
+{
+	g_sensitivity = sensitivity;
+	g_specificity = specificity;
+}
+
 /* ReplicatedNonDilutionLattice::response_prob,
  * src/core/model/replicated_lattice.cpp:8-14, and
  * ReplicatedDilutionLattice::response_prob, :17-28.  `subjects` is the
@@ -63,13 +77,12 @@ ORC_EXPORT double orc_response_prob(int dilution, int subjects, int variants, ui
 	double ret = 1.0;
 	if (!dilution)
 	{
-		const double negative_response = BGT_NON_DILUTION_NEGATIVE;
+		const double spec = g_specificity, sens = g_sensitivity;
 		for (int v = 0; v < variants; v++)
 		{
 			const uint32_t shifted = (uint32_t)((uint64_t)s >> (v * subjects));
 			const int bit = (r & (1u << v)) != 0;
-			ret *= ((e & shifted) == e) ? (bit == 0 ? (1.0 - negative_response) : negative_response)
-										: (bit == 0 ? negative_response : (1.0 - negative_response));
+			ret *= ((e & shifted) == e) ? (bit == 0 ? (1.0 - spec) : spec) : (bit == 0 ? sens : (1.0 - sens));
 		}
 		return ret;
 	}
@@ -410,8 +423,8 @@ ORC_EXPORT int orc_session(int dilution, int subjects, int variants, const doubl
 	for (int stage = 0; stage < stages; stage++)
 	{
 		const uint32_t e = orc_select(post, subjects, variants, selector, scratch);
-		const uint32_t r = bgt_session_sample_response(dilution, subjects, variants, e, true_state, alpha, h, seed,
-													   session, (uint32_t)stage);
+		const uint32_t r = bgt_session_sample_response(dilution, subjects, variants, e, true_state, alpha, h,
+													   g_specificity, g_sensitivity, seed, session, (uint32_t)stage);
 		orc_update(dilution, subjects, variants, post, post, e, r, dil, subjects + 1, 1);
 		orc_classify(post, atoms, up, lo, &pos, &neg);
 		experiments[stage] = e;
@@ -873,5 +886,6 @@ ORC_EXPORT void orc_sample_prior(int atoms, double lo, double hi, uint64_t seed,
 ORC_EXPORT uint32_t orc_sample_response(int dilution, int subjects, int variants, uint32_t e, uint32_t s, double alpha,
 										double h, uint64_t seed, uint64_t session, uint32_t stage)
 {
-	return bgt_session_sample_response(dilution, subjects, variants, e, s, alpha, h, seed, session, stage);
+	return bgt_session_sample_response(dilution, subjects, variants, e, s, alpha, h, g_specificity, g_sensitivity,
+									   seed, session, stage);
 }

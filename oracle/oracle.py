@@ -15,6 +15,7 @@ use this module, and only as the checker.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import os
 import subprocess
@@ -110,6 +111,26 @@ class Oracle:
         L.orc_sample_response.argtypes = [c_int, c_int, c_int, c_uint32, c_uint32, c_double, c_double, c_uint64,
                                           c_uint64, c_uint32]
         L.orc_sample_response.restype = c_uint32
+        L.orc_set_test_accuracy.argtypes = [c_double, c_double]
+        L.orc_set_test_accuracy.restype = None
+
+    # non-dilution test accuracy ---------------------------------------------
+    REFERENCE_ACCURACY = 0.99  # replicated_lattice.cpp:6, both sensitivity and specificity
+
+    def set_test_accuracy(self, sensitivity=REFERENCE_ACCURACY, specificity=REFERENCE_ACCURACY):
+        """Non-dilution likelihood P(positive | a positive pooled) = sensitivity,
+        P(negative | none pooled) = specificity for every later call (the
+        defaults are the reference's fixed model)."""
+        self.lib.orc_set_test_accuracy(float(sensitivity), float(specificity))
+
+    @contextlib.contextmanager
+    def test_accuracy(self, sensitivity, specificity):
+        """Runs the block with the given accuracy, then restores the reference's."""
+        self.set_test_accuracy(sensitivity, specificity)
+        try:
+            yield self
+        finally:
+            self.set_test_accuracy()
 
     # model -----------------------------------------------------------------
     def dilution_table(self, n, alpha=0.99, h=0.005):

@@ -236,7 +236,8 @@ int ref_session(int type, int n, int k, const double *pi0, int selector, double 
 		for (int stage = 0; stage < stages; stage++)
 		{
 			const uint32_t e = lattice->select_experiment(static_cast<bgt::SelectorType>(selector));
-			const uint32_t r = bgt_session_sample_response(type == 4, n, k, e, true_state, alpha, h, seed, session,
+			const uint32_t r = bgt_session_sample_response(type == 4, n, k, e, true_state, alpha, h, BGT_NON_DILUTION_NEGATIVE,
+														   BGT_NON_DILUTION_NEGATIVE, seed, session,
 														   static_cast<uint32_t>(stage));
 			lattice->update_probs_in_place(e, r, rows);
 			lattice->update_metadata(up, lo);

@@ -144,6 +144,12 @@ int main(int argc, char **argv)
 	expect_near(lattice.response_probability(1, 1, 3), 0.99, 1e-15, "response probability, contained");
 	expect_near(lattice.response_probability(1, 1, 2), 0.01, 1e-15, "response probability, not contained");
 	expect_near(lattice.response_probability(3, 0, 1), 0.99, 1e-15, "response probability, positive");
+	{
+		bgt::Lattice accurate(bgt::LatticeType::replicated_non_dilution, 2, prior);
+		accurate.set_test_accuracy(0.95, 0.98);
+		expect_near(accurate.response_probability(1, 1, 3), 0.98, 1e-15, "specificity, contained pool");
+		expect_near(accurate.response_probability(1, 0, 2), 0.95, 1e-15, "sensitivity, pooled positive");
+	}
 	expect_equal(lattice.select_experiment(), 3, "auto selection");
 	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bha), 3, "Op-BHA selection");
 	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bbpa), 3, "Op-BBPA selection");
@@ -191,6 +197,19 @@ int main(int argc, char **argv)
 	expect_near(st.unclassified_probability, 0.206, 1e-12, "single-subject unclassified");
 	expect_near(st.expected_stages, 1.0, 1e-12, "single-subject expected stages");
 	expect_near(st.expected_tests, 1.0, 1e-12, "single-subject expected tests");
+	{
+		bgt::SimulationConfig acc = cfg;
+		acc.test_accuracy = bgt::TestAccuracy{0.95, 0.98};
+		const bgt::TreeStats sa = bgt::run_simulation(acc).stats;
+		expect_equal(sa.total_leaves, 2, "accuracy: leaves");
+		expect_near(sa.correct_probability + sa.incorrect_probability + sa.unclassified_probability, 1.0, 1e-12,
+					"accuracy: outcomes sum to 1");
+		expect_equal(std::abs(sa.correct_probability - st.correct_probability) > 1e-6, 1,
+					 "accuracy: the likelihood reached the tree");
+		acc.lattice_type = bgt::LatticeType::replicated_dilution;
+		expect_error([&] { bgt::run_simulation(acc); }, bgt::StatusCode::invalid_argument,
+					 "accuracy on a dilution lattice");
+	}
 
 	// Reports and progress files.
 	const std::filesystem::path dir =

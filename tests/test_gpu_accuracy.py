@@ -1,0 +1,142 @@
+"""Non-dilution test accuracy other than the reference's fixed 0.99 / 0.99
+(sensitivity 0.95, specificity 0.98 in the headline workloads): updates,
+response probabilities, device sessions and trees against the oracle under
+the same accuracy, and 0.99 / 0.99 set explicitly against the reference's
+own path, bit for bit."""
+import numpy as np
+import pytest
+
+import bayesiangrouptesting_gb300 as bgt
+from conftest import assert_posterior_close
+
+pytestmark = pytest.mark.gpu
+
+SENS, SPEC = 0.95, 0.98
+TOL = 1e-12  # FP64 posterior / TreeStats tolerance
+
+
+def _tree(n, k, pi0, depth, branch=0.0, accuracy=None, selector=0, thr=0.01):
+    cfg = bgt.SimulationConfig(
+        subjects=n, variants=k, prior=list(pi0),
+        options=bgt.SimulationOptions(search_depth=depth, branch_threshold=branch, threshold_up=thr, threshold_lo=thr,
+                                      selector=bgt.SelectorType(selector), provider=bgt.Provider.cuda),
+        test_accuracy=accuracy)
+    return bgt.run_simulation(cfg).stats.as_array()
+
+
+def _check_stats(got, want):
+    assert got[0] == want[0], (got, want)
+    np.testing.assert_allclose(got[1:], want[1:], rtol=TOL, atol=TOL)
+
+
+@pytest.mark.parametrize("n,k", [(12, 1), (5, 2), (4, 3)])
+def test_updates_and_response_probability(gpu, oracle, n, k):
+    rng = np.random.default_rng(500 + n + k)
+    pi0 = rng.uniform(0.01, 0.2, n * k)
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0, k)
+    lat.set_test_accuracy(SENS, SPEC)
+    rev = (lambda v: bgt.reverse_bits(v, n)) if k == 1 else (lambda v: v)
+    with oracle.test_accuracy(SENS, SPEC):
+        post = oracle.prior(pi0)
+        for step in range(5):
+            e = int(rng.integers(1, 1 << n))
+            r = int(rng.integers(0, 1 << k))
+            post = oracle.update(0, n, k, post, e, r, in_place=True)
+            lat.update(rev(e), r)
+            assert_posterior_close(lat.posterior(), post, step + 1)
+        for _ in range(100):
+            e = int(rng.integers(1, 1 << n))
+            r = int(rng.integers(0, 1 << k))
+            s = int(rng.integers(0, 1 << (n * k)))
+            want = oracle.response_prob(0, n, k, e, r, s)
+            assert abs(lat.response_probability(rev(e), r, rev(s)) - want) <= 1e-15
+
+
+def test_accuracy_changes_the_likelihood(gpu):
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 2, [0.2, 0.4])
+    assert abs(lat.response_probability(1, 1, 3) - 0.99) <= 1e-15
+    lat.set_test_accuracy(SENS, SPEC)
+    assert abs(lat.response_probability(1, 1, 3) - SPEC) <= 1e-15          # contained, negative
+    assert abs(lat.response_probability(1, 0, 3) - (1 - SPEC)) <= 1e-15
+    assert abs(lat.response_probability(1, 0, 2) - SENS) <= 1e-15          # a pooled positive, positive
+    assert abs(lat.response_probability(1, 1, 2) - (1 - SENS)) <= 1e-15
+
+
+def test_pending_update_keeps_its_accuracy(gpu, oracle):
+    n = 6
+    pi0 = np.linspace(0.05, 0.2, n)
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0)
+    lat.update(bgt.reverse_bits(5, n), 1)       # made under the reference model, applied lazily
+    lat.set_test_accuracy(SENS, SPEC)
+    lat.update(bgt.reverse_bits(12, n), 0)
+    post = oracle.update(0, n, 1, oracle.prior(pi0), 5, 1, in_place=True)
+    with oracle.test_accuracy(SENS, SPEC):
+        post = oracle.update(0, n, 1, post, 12, 0, in_place=True)
+    assert_posterior_close(lat.posterior(), post, 2)
+
+
+def test_invalid_accuracy_is_rejected(gpu):
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 3, [0.1, 0.2, 0.3])
+    for sens, spec in ((1.5, 0.9), (0.9, -0.1), (float("nan"), 0.9)):
+        with pytest.raises(ValueError):
+            lat.set_test_accuracy(sens, spec)
+    dil = bgt.Lattice(bgt.LatticeType.replicated_dilution, 3, [0.1, 0.2, 0.3])
+    with pytest.raises(ValueError):
+        dil.set_test_accuracy(SENS, SPEC)
+    lib = bgt.api.load()
+    assert lib.bgt_gpu_lattice_set_test_accuracy(dil.handle, SENS, SPEC) == 2
+    assert lib.bgt_gpu_lattice_set_test_accuracy(lat.handle, 2.0, SPEC) == 2
+
+
+@pytest.mark.parametrize("n,k,selector", [(10, 1, 1), (15, 1, 2), (4, 2, 2), (3, 3, 2)])
+def test_device_session(gpu, oracle, n, k, selector):
+    rng = np.random.default_rng(600 + n)
+    pi0 = rng.uniform(0.01, 0.10, n * k)
+    truth = int(rng.integers(0, 1 << (n * k))) | int(rng.integers(0, 1 << (n * k)))
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0, k)
+    lat.set_test_accuracy(SENS, SPEC)
+    got = lat.run_session(8, truth, seed=7, session=2, selector=selector)
+    with oracle.test_accuracy(SENS, SPEC):
+        want = oracle.session(0, n, k, pi0, 8, 7, 2, truth, selector=selector)
+    for key in ("experiments", "responses", "pos", "neg"):
+        np.testing.assert_array_equal(got[key], want[key])
+    assert_posterior_close(lat.posterior(), want["posterior"], 8)
+
+
+@pytest.mark.parametrize("n,k,depth,branch,thr", [
+    (8, 1, 5, 0.0, 0.01),    # leaf sums of the device-built tree
+    (8, 1, 5, 1e-4, 0.01),   # the per-true-state sweep with pruning
+    (10, 1, 6, 0.0, 0.01),
+    (5, 1, 17, 0.0, 0.1),    # 2^17 slots: the host-driven level loop (30 leaves)
+    (3, 2, 3, 0.0, 0.01),    # multinomial Op-BBPA
+    (3, 2, 3, 1e-3, 0.01),
+])
+def test_tree(gpu, oracle, n, k, depth, branch, thr):
+    rng = np.random.default_rng(700 + n + depth)
+    pi0 = rng.uniform(0.01, 0.15, n * k)
+    got = _tree(n, k, pi0, depth, branch, bgt.TestAccuracy(SENS, SPEC), thr=thr)
+    with oracle.test_accuracy(SENS, SPEC):
+        want = oracle.run_simulation(0, n, k, pi0, depth, up=thr, lo=thr, branch=branch)
+    _check_stats(got, want)
+    # the reference model differs: the accuracy really reached the tree
+    ref = _tree(n, k, pi0, depth, branch, thr=thr)
+    assert ref[0] != got[0] or np.max(np.abs(ref[1:] - got[1:])) > 1e-6
+
+
+@pytest.mark.parametrize("branch", [0.0, 1e-4])
+def test_reference_accuracy_is_bit_exact(gpu, branch):
+    rng = np.random.default_rng(800)
+    n = 9
+    pi0 = rng.uniform(0.01, 0.15, n)
+    explicit = _tree(n, 1, pi0, 5, branch, bgt.TestAccuracy(0.99, 0.99))
+    reference = _tree(n, 1, pi0, 5, branch)
+    np.testing.assert_array_equal(explicit, reference)
+    a = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0)
+    b = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, pi0)
+    b.set_test_accuracy(0.99, 0.99)
+    for e, r in ((3, 1), (40, 0), (257, 1)):
+        a.update(e, r)
+        b.update(e, r)
+    np.testing.assert_array_equal(a.posterior(), b.posterior())
+    with pytest.raises(ValueError):
+        _tree(n, 1, pi0, 3, 0.0, bgt.TestAccuracy(1.2, 0.9))

@@ -152,3 +152,29 @@ def test_host_response_stream_matches_oracle(oracle):
         alpha = 0.01 if dil else 0.99
         want = oracle.lib.orc_sample_response(1 if dil else 0, n, 1, e, s, alpha, 0.005, 7, t, t % 40)
         assert bench.session_response(dil, n, e, s, alpha, 0.005, 7, t, t % 40) == want
+
+
+def test_test_accuracy_extension(oracle):
+    # Non-dilution accuracy other than the reference's 0.99 / 0.99: the same
+    # formula with specificity (contained pool) and sensitivity (a pooled
+    # positive); the context restores the reference model.
+    e, full, partial = 3, 3, 2  # internal order, n = 2: pool {0, 1}
+    base = [oracle.response_prob(0, 2, 1, e, r, s) for r in (0, 1) for s in (full, partial)]
+    with oracle.test_accuracy(0.95, 0.98):
+        assert abs(oracle.response_prob(0, 2, 1, e, 1, full) - 0.98) < 1e-15
+        assert abs(oracle.response_prob(0, 2, 1, e, 0, full) - (1 - 0.98)) < 1e-15
+        assert abs(oracle.response_prob(0, 2, 1, e, 0, partial) - 0.95) < 1e-15
+        assert abs(oracle.response_prob(0, 2, 1, e, 1, partial) - (1 - 0.95)) < 1e-15
+        # two variants multiply their factors
+        s = full | (partial << 2)
+        assert abs(oracle.response_prob(0, 2, 2, e, 0b01, s) - 0.98 * 0.95) < 1e-15
+        # dilution lattices keep their table
+        assert abs(oracle.response_prob(1, 2, 1, 3, 1, 3) - 0.99) < 1e-12
+    assert [oracle.response_prob(0, 2, 1, e, r, s) for r in (0, 1) for s in (full, partial)] == base
+    # 0.99 / 0.99 set explicitly is the reference model bit for bit
+    pi0 = [0.1, 0.2, 0.3, 0.05]
+    want = oracle.run_simulation(0, 4, 1, pi0, 3, branch=1e-4)
+    with oracle.test_accuracy(0.99, 0.99):
+        np.testing.assert_array_equal(oracle.run_simulation(0, 4, 1, pi0, 3, branch=1e-4), want)
+    with oracle.test_accuracy(0.95, 0.98):
+        assert np.max(np.abs(oracle.run_simulation(0, 4, 1, pi0, 3, branch=1e-4) - want)) > 1e-6
