@@ -43,6 +43,9 @@ H = 0.005
 PRIOR_LO, PRIOR_HI = 0.005, 0.10
 THRESHOLD = 0.01
 SEED = 20260624
+# Non-dilution test accuracy of the n=20 tree and the n=10 x k=3 multinomial
+# workloads (the reference's own model is 0.99 / 0.99).
+SENSITIVITY, SPECIFICITY = 0.95, 0.98
 METRIC = "lattice stages/s"
 WORKLOAD = "binary dilution lattice n=24 (2^24 FP64 states), 32-stage Op-BBPA select->update->classify session"
 
@@ -408,9 +411,10 @@ def run_serving(count: int, fp32: bool = False, plain: bool = True):
 
 def run_tree(reps: int = 5):
     """Batched tree simulation: binary non-dilution lattice n=20
-    (pi0 ~ U[0.01, 0.15]), Op-BHA to search depth 8, TreeStats over all 2^20
-    true states, through run_simulation (one graph replay per tree), against
-    the oracle port of the reference CPU provider on one host core."""
+    (pi0 ~ U[0.01, 0.15]), sensitivity 0.95 and specificity 0.98, Op-BHA to
+    search depth 8, TreeStats over all 2^20 true states, through
+    run_simulation (one graph replay per tree), against the oracle port of the
+    reference CPU provider (same accuracy) on one host core."""
     import bayesiangrouptesting_gb300 as bgt
     from oracle.oracle import Oracle
 
@@ -418,7 +422,8 @@ def run_tree(reps: int = 5):
     rng = np.random.default_rng(SEED + 3)
     pi0 = rng.uniform(0.01, 0.15, n)
     cfg = bgt.SimulationConfig(subjects=n, prior=list(pi0),
-                               options=bgt.SimulationOptions(search_depth=depth, provider=bgt.Provider.cuda))
+                               options=bgt.SimulationOptions(search_depth=depth, provider=bgt.Provider.cuda),
+                               test_accuracy=bgt.TestAccuracy(SENSITIVITY, SPECIFICITY))
     bgt.run_simulation(cfg)  # builds and captures the graph, tunes the block width
     times = []
     for _ in range(reps):
@@ -435,11 +440,13 @@ def run_tree(reps: int = 5):
         t0 = time.perf_counter()
         swept = bgt.run_simulation(cfg).stats.as_array()
         sweep_times.append(time.perf_counter() - t0)
-    t0 = time.perf_counter()
-    want = Oracle().run_simulation(0, n, 1, pi0, depth)
-    cpu_s = time.perf_counter() - t0
-    return {"workload": f"binary non-dilution n={n}, Op-BHA, search depth {depth}, TreeStats over 2^{n} true "
-                        "states (device-built tree, one CUDA graph replay)",
+    with Oracle().test_accuracy(SENSITIVITY, SPECIFICITY) as orc:
+        t0 = time.perf_counter()
+        want = orc.run_simulation(0, n, 1, pi0, depth)
+        cpu_s = time.perf_counter() - t0
+    return {"workload": f"binary non-dilution n={n}, sensitivity {SENSITIVITY}, specificity {SPECIFICITY}, Op-BHA, "
+                        f"search depth {depth}, TreeStats over 2^{n} true states (device-built tree, one CUDA "
+                        "graph replay)",
             "ms_per_tree": 1e3 * statistics.median(times), "leaves": int(got[0]),
             "ms_per_tree_true_state_sweep": 1e3 * statistics.median(sweep_times),
             "max_abs_diff_sweep_vs_leaf_sums": float(np.max(np.abs(swept - got))),
@@ -465,10 +472,11 @@ def run_precision(stages: int = 16):
     truth = int(sum(1 << a for a in range(n * k) if draws[a] >= pi0[a]))
     t = bgt.LatticeType.replicated_non_dilution
     out = {"workload": f"multinomial non-dilution lattice n={n} x k={k} (2^30 states), {stages}-stage Op-BBPA "
-                       "session; likelihood 0.99/0.99 (the reference model)"}
+                       f"session; sensitivity {SENSITIVITY}, specificity {SPECIFICITY} per variant"}
     lats = {}
     for name, prec in (("fp64", bgt.Precision.float64), ("fp32", bgt.Precision.float32)):
         lat = bgt.Lattice(t, n, pi0, variants=k, precision=prec)
+        lat.set_test_accuracy(SENSITIVITY, SPECIFICITY)
         lat.run_session(2, truth, seed=SEED, session=0)  # warm-up
         times = []
         for rep in range(3):
