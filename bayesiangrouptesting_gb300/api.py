@@ -724,6 +724,17 @@ class Lattice:
         _call(self._lib.bgt_gpu_lattice_select(self._handle, int(selector), ctypes.byref(out)))
         return self._to_public(out.value)
 
+    def select_experiments(self, k: int, selector: SelectorType = SelectorType.op_bha) -> list:
+        """Lattice::select_experiments (src/core/lattice_api.cpp:116-168): the
+        Op-BHA selection, then greedy k-lookahead candidates, public order."""
+        if k < 0:
+            raise ValueError("k must be non-negative.")
+        if k == 0:
+            return []
+        out = (ctypes.c_uint32 * k)()
+        _call(self._lib.bgt_gpu_lattice_select_experiments(self._handle, k, int(selector), out))
+        return [self._to_public(int(v)) for v in out]
+
     def update(self, experiment: int, response: int, dilution: Optional[DilutionTable] = None) -> None:
         if _uses_dilution(self._type) and dilution is None:
             raise ValueError("dilution table is required for dilution models.")

@@ -402,6 +402,11 @@ struct bgt_gpu_lattice
 	unsigned long long *ftab = nullptr; // k >= 2 feature masses
 	unsigned int *sess_out = nullptr; // 4 * max stages
 	int sess_capacity = 0;
+	// k-lookahead scratch, allocated on first use: down-set sums (2^n u64),
+	// per-CTA results, intersection masks and the winner.
+	unsigned long long *la_d = nullptr, *la_scratch = nullptr;
+	unsigned int *la_masks = nullptr, *la_result = nullptr;
+	int la_blocks = 0;
 	bool have_dilution = false;
 	// Host-side view of the device pipeline.
 	bool k1_pending = true;   // a K1 must run before the zeta partial sums are current
@@ -428,6 +433,10 @@ struct bgt_gpu_lattice
 		cudaFree(scratch_u64);
 		cudaFree(ftab);
 		cudaFree(sess_out);
+		cudaFree(la_d);
+		cudaFree(la_scratch);
+		cudaFree(la_masks);
+		cudaFree(la_result);
 		if (own_stream)
 			cudaStreamDestroy(own_stream);
 	}
@@ -1039,6 +1048,93 @@ int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t expe
 	}
 	*out = p;
 	return BGT_GPU_OK;
+}
+
+int bgt_gpu_lattice_select_experiments(bgt_gpu_lattice *lattice, int count, int selector, uint32_t *experiments)
+{
+	if (!lattice || (count > 0 && !experiments))
+	{
+		set_error("null lattice or output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	// Argument checks of Lattice::select_experiments (src/core/lattice_api.cpp:116-137).
+	if (count < 0)
+	{
+		set_error("k must be non-negative.");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (count == 0)
+		return BGT_GPU_OK;
+	const int k = lattice->g.k;
+	const int resolved = selector == 0 ? (k == 1 ? 1 : 2) : selector;
+	if (resolved == 2)
+	{
+		if (count != 1)
+		{
+			set_error("Op-BBPA currently selects one experiment at a time.");
+			return BGT_GPU_MISSING_DILUTION;
+		}
+		return bgt_gpu_lattice_select(lattice, selector, experiments);
+	}
+	if (resolved != 1 || k != 1)
+	{
+		set_error("Op-BHA multi-experiment selection is only supported for binary lattices.");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	if (count > kLookaheadMax)
+	{
+		set_error("at most " + std::to_string(kLookaheadMax) + " lookahead experiments per call");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (const int rc = bgt_gpu_lattice_select(lattice, 1, &experiments[0]))
+		return rc;
+	if (count == 1)
+		return BGT_GPU_OK;
+	return guarded([&]() -> int {
+		const int n = lattice->g.n;
+		const size_t states = size_t{1} << n;
+		if (!lattice->la_d)
+		{
+			lattice->la_blocks = lookahead_score_blocks(n);
+			cuda_check(cudaMalloc(&lattice->la_d, states * sizeof(unsigned long long)), "alloc lookahead sums");
+			cuda_check(cudaMalloc(&lattice->la_scratch, 3 * static_cast<size_t>(lattice->la_blocks) *
+															 sizeof(unsigned long long)),
+					   "alloc lookahead scratch");
+			cuda_check(cudaMalloc(&lattice->la_masks, (size_t{1} << (kLookaheadMax - 1)) * sizeof(unsigned int)),
+					   "alloc lookahead masks");
+			cuda_check(cudaMalloc(&lattice->la_result, sizeof(unsigned int)), "alloc lookahead result");
+		}
+		if (lattice->update_pending || lattice->k1_pending)
+			lattice->run_k1();
+		const double z = lattice->get_field<double>(offsetof(LatticeDev, z_norm));
+		lattice->check_device_error();
+		if (!(z > 0.0) || !std::isfinite(z))
+			throw CudaFailure("posterior normalising constant is zero");
+		// The values sum to z: at scale 2^(61 - ilogb z) their fixed-point
+		// total stays below 2^62.
+		launch_downset(lattice->q, lattice->precision == BGT_GPU_FP32 ? 1 : 0, n, 61 - std::ilogb(z), lattice->la_d,
+					   lattice->stream);
+		const unsigned int full = (1u << n) - 1u;
+		std::vector<unsigned int> masks;
+		for (int step = 1; step < count; step++)
+		{
+			// masks[J] = the subjects common to the experiments in J.
+			masks.assign(size_t{1} << step, full);
+			for (size_t J = 1; J < masks.size(); J++)
+				masks[J] = masks[J & (J - 1)] & experiments[__builtin_ctzll(J)];
+			cuda_check(cudaMemcpyAsync(lattice->la_masks, masks.data(), masks.size() * sizeof(unsigned int),
+									   cudaMemcpyHostToDevice, lattice->stream),
+					   "lookahead masks up");
+			launch_lookahead_select(lattice->la_d, n, step + 1, lattice->la_masks, lattice->la_scratch,
+									lattice->la_blocks, lattice->la_result, lattice->stream);
+			unsigned int e = 0;
+			cuda_check(cudaMemcpyAsync(&e, lattice->la_result, sizeof(e), cudaMemcpyDeviceToHost, lattice->stream),
+					   "lookahead result down");
+			cuda_check(cudaStreamSynchronize(lattice->stream), "lookahead sync");
+			experiments[step] = e;
+		}
+		return BGT_GPU_OK;
+	});
 }
 
 int bgt_gpu_lattice_set_test_accuracy(bgt_gpu_lattice *lattice, double sensitivity, double specificity)

@@ -63,6 +63,19 @@ void launch_k2(LatticeDev *states, int count, const LatticeGeometry &g, cudaStre
 // is the map's total work items.
 void launch_k1_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream);
 void launch_k2_map(LatticeDev *states, const WorkMap &wm, long long items, cudaStream_t stream);
+// Greedy k-lookahead (lookahead.cu).  At most kLookaheadMax experiments per
+// call (2^kLookaheadMax response groups per candidate).
+constexpr int kLookaheadMax = 10;
+// floor(q * 2^scale) of the 2^n posterior values (FP32 when fp32), then the
+// in-place down-set sums D(E) = sum over s subset of E, into d (2^n u64).
+void launch_downset(const void *q, int fp32, int n, int scale, unsigned long long *d, cudaStream_t stream);
+// CTAs of the scoring launch for n subjects (its scratch holds 3 u64 per CTA).
+int lookahead_score_blocks(int n);
+// The candidate of least lookahead score against the previous experiments,
+// given their 2^(m-1) intersection masks (masks[0] = every subject), lowest
+// public index on ties; writes its internal index to *result (device).
+void launch_lookahead_select(const unsigned long long *d, int n, int m, const unsigned int *masks,
+							 unsigned long long *scratch, int blocks, unsigned int *result, cudaStream_t stream);
 size_t k1_smem_bytes();
 size_t k2_smem_bytes(int hbits);
 int sm_count();

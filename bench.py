@@ -455,6 +455,48 @@ def run_tree(reps: int = 5):
             "max_abs_stats_diff_vs_oracle": float(np.max(np.abs(got - want)))}
 
 
+def run_lookahead(reps: int = 5):
+    """Greedy k-lookahead (Lattice::select_experiments): n=20 and n=24 binary
+    non-dilution lattices after four updates, 4 and 3 experiments per call;
+    and n=12, 3 experiments, beside the oracle port of the reference's brute
+    force on one host core (its cost grows as 4^n: n=12 is what it finishes
+    in seconds)."""
+    import bayesiangrouptesting_gb300 as bgt
+    from oracle.oracle import Oracle
+
+    def lattice(n, seed):
+        rng = np.random.default_rng(seed)
+        lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, rng.uniform(0.01, 0.15, n))
+        for _ in range(4):
+            lat.update(int(rng.integers(1, 1 << n)), int(rng.integers(0, 2)))
+        lat.select_experiments(2)  # first call allocates the scratch
+        return lat
+
+    def timed(lat, count):
+        times = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            got = lat.select_experiments(count)
+            times.append(time.perf_counter() - t0)
+        return got, 1e3 * statistics.median(times)
+
+    out = {"workload": "k-lookahead select_experiments, binary non-dilution lattice after 4 updates"}
+    for n, count in ((20, 4), (24, 3)):
+        _, ms = timed(lattice(n, SEED + n), count)
+        out[f"ms_n{n}_k{count}"] = ms
+    small = lattice(12, SEED + 12)
+    got, ms = timed(small, 3)
+    post = small.posterior()
+    t0 = time.perf_counter()
+    want = Oracle().select_experiments(post, 12, 3)
+    cpu_s = time.perf_counter() - t0
+    out["ms_n12_k3"] = ms
+    out["cpu_baseline"] = {"seconds": cpu_s, "cores": 1, "kind": "port", "sample": "n=12, 3 experiments, once"}
+    out["speedup_vs_cpu_n12"] = 1e3 * cpu_s / ms
+    out["n12_equal_to_oracle"] = got == want
+    return out
+
+
 def run_precision(stages: int = 16):
     """Multinomial lattice n = 10 subjects x k = 3 variants (2^30 states):
     a 16-stage Op-BBPA session in FP64 and in FP32 storage (stages/s each),
@@ -611,6 +653,9 @@ def run_gpu(args, world, rank, local):
     tree = None
     if rank == 0 and world == 1 and not args.no_tree:
         tree = run_tree()
+    lookahead = None
+    if rank == 0 and world == 1 and not args.no_lookahead:
+        lookahead = run_lookahead()
     serving = None
     if rank == 0 and world == 1 and args.serve_sessions > 0:
         with ClockSampler(local) as serve_clocks:
@@ -639,6 +684,7 @@ def run_gpu(args, world, rank, local):
         "serving": serving,
         "precision": precision,
         "tree": tree,
+        "lookahead": lookahead,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -659,6 +705,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP64-vs-FP32 n=10 x k=3 measurement")
     ap.add_argument("--no-tree", action="store_true", help="skip the n=20 depth-8 tree measurement")
+    ap.add_argument("--no-lookahead", action="store_true", help="skip the k-lookahead measurement")
     ap.add_argument("--profile-steps", type=int, default=10,
                     help="sessions run after the timed region with per-pass CUDA events (roofline split)")
     ap.add_argument("--serve-sessions", type=int, default=SERVE_SESSIONS,

@@ -281,6 +281,24 @@ class Lattice
 		detail::check(bgt_gpu_lattice_upset_mass(h_, to_internal(experiment), &out));
 		return out;
 	}
+	// Lattice::select_experiments (src/core/lattice_api.cpp:116-168): the
+	// Op-BHA selection, then greedy lookahead candidates (public order).
+	std::vector<state_t> select_experiments(int k, SelectorType selector = SelectorType::op_bha) const
+	{
+		if (k < 0)
+			throw std::invalid_argument("k must be non-negative.");
+		std::vector<state_t> out(static_cast<std::size_t>(k));
+		if (k == 0)
+			return out;
+		std::vector<uint32_t> raw(static_cast<std::size_t>(k));
+		const int rc = bgt_gpu_lattice_select_experiments(h_, k, static_cast<int>(selector), raw.data());
+		if (rc == BGT_GPU_MISSING_DILUTION)
+			throw std::invalid_argument(bgt_gpu_last_error());
+		detail::check(rc);
+		for (std::size_t i = 0; i < out.size(); i++)
+			out[i] = to_internal(raw[i]);
+		return out;
+	}
 	// Extension: the non-dilution likelihood of later updates
 	// (bgt_gpu_lattice_set_test_accuracy).
 	void set_test_accuracy(host_probability_t sensitivity, host_probability_t specificity)

@@ -163,6 +163,18 @@ BGT_GPU_API int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t ex
 BGT_GPU_API int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
 													 uint32_t true_state, double **dilution, double *out);
 
+/* Lattice::select_experiments (include/bgt/lattice.hpp:54;
+ * src/core/lattice_api.cpp:116-168): `count` experiments into `experiments`
+ * (internal bit order).  Op-BHA (selector 1, or 0 on a binary lattice): the
+ * lattice's Op-BHA selection, then greedily the candidate whose response
+ * groups are closest to equal mass given the ones before it (the reference's
+ * brute-force score, here exact), the lowest public (bit-reversed) index on
+ * ties.  Op-BBPA: count must be 1.  Status 1 for the reference's argument
+ * errors (count < 0, Op-BBPA with count != 1, Op-BHA on a multinomial
+ * lattice), 2 above 10 experiments. */
+BGT_GPU_API int bgt_gpu_lattice_select_experiments(bgt_gpu_lattice *lattice, int count, int selector,
+												   uint32_t *experiments);
+
 /* Non-dilution test accuracy (an extension: the reference fixes both at 0.99,
  * src/core/model/replicated_lattice.cpp:6-14).  Later updates, sessions and
  * response_probability use

@@ -395,6 +395,77 @@ ORC_EXPORT uint32_t orc_select(const double *post, int subjects, int variants, i
 	return orc_bbpa(post, subjects, variants, 1.0 / (double)(1 << variants), scratch, NULL);
 }
 
+/* ------------------------------------------------------- k-lookahead */
+
+static uint32_t orc_reverse(uint32_t v, int bits)
+{
+	uint32_t r = 0;
+	for (int i = 0; i < bits; i++)
+		if (v & (1u << i))
+			r |= 1u << (bits - 1 - i);
+	return r;
+}
+
+/* The brute-force score of Lattice::select_experiments
+ * (src/core/lattice_api.cpp:145-158) for the public experiments exps[0..m):
+ * states grouped by set_group_index (:33-44: bit i set when the state is a
+ * subset of experiment i, is_up_set :28-31), group masses summed over public
+ * states in ascending order, score = sum over groups of |mass - 1/2^m|.
+ * `post` is the normalised posterior in internal order (public state p is
+ * internal reverse(p)); `mass` holds 2^m doubles. */
+ORC_EXPORT double orc_lookahead_score(const double *post, int subjects, int m, const uint32_t *exps, double *mass)
+{
+	const uint32_t total = 1u << subjects;
+	memset(mass, 0, sizeof(double) << m);
+	for (uint32_t state = 0; state < total; state++)
+	{
+		int g = 0;
+		for (int i = 0; i < m; i++)
+			if ((exps[i] & state) == state)
+				g |= 1 << i;
+		mass[g] += post[orc_reverse(state, subjects)];
+	}
+	const double target = 1.0 / (double)(1 << m);
+	double score = 0.0;
+	for (int g = 0; g < (1 << m); g++)
+		score += fabs(mass[g] - target);
+	return score;
+}
+
+/* Lattice::select_experiments(count, op_bha), src/core/lattice_api.cpp:116-168,
+ * for a binary lattice in public order: the first experiment is `first`
+ * (the lattice's Op-BHA selection, public order), each later one the
+ * candidate 1 .. 2^n - 1 of least score given the ones before it, the
+ * lowest candidate on ties.  Returns 0, or 4 when out of memory. */
+ORC_EXPORT int orc_select_experiments(const double *post, int subjects, int count, uint32_t first, uint32_t *out)
+{
+	if (count <= 0)
+		return 0;
+	double *mass = (double *)malloc(sizeof(double) << count);
+	if (!mass)
+		return 4;
+	out[0] = first;
+	const uint32_t total = 1u << subjects;
+	for (int step = 1; step < count; step++)
+	{
+		double best = INFINITY;
+		uint32_t best_e = 0;
+		for (uint32_t candidate = 1; candidate < total; candidate++)
+		{
+			out[step] = candidate;
+			const double score = orc_lookahead_score(post, subjects, step + 1, out, mass);
+			if (score < best)
+			{
+				best = score;
+				best_e = candidate;
+			}
+		}
+		out[step] = best_e;
+	}
+	free(mass);
+	return 0;
+}
+
 /* ---------------------------------------------------------------- session */
 
 /* One adaptive session in the bgt::Lattice call order

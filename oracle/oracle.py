@@ -111,6 +111,10 @@ class Oracle:
         L.orc_sample_response.argtypes = [c_int, c_int, c_int, c_uint32, c_uint32, c_double, c_double, c_uint64,
                                           c_uint64, c_uint32]
         L.orc_sample_response.restype = c_uint32
+        L.orc_lookahead_score.argtypes = [_dp, c_int, c_int, _up, _dp]
+        L.orc_lookahead_score.restype = c_double
+        L.orc_select_experiments.argtypes = [_dp, c_int, c_int, c_uint32, _up]
+        L.orc_select_experiments.restype = c_int
         L.orc_set_test_accuracy.argtypes = [c_double, c_double]
         L.orc_set_test_accuracy.restype = None
 
@@ -212,6 +216,24 @@ class Oracle:
         pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
         return int(self.lib.orc_sample_truth(len(pi0), _ptr(pi0), seed, session))
 
+    # k-lookahead (public order) -----------------------------------------------
+    def lookahead_score(self, post, n, exps):
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        exps = np.ascontiguousarray(exps, dtype=np.uint32)
+        mass = np.empty(1 << len(exps))
+        return self.lib.orc_lookahead_score(_ptr(post), n, len(exps), _ptr(exps, _up), _ptr(mass))
+
+    def select_experiments(self, post, n, count):
+        """Lattice::select_experiments(count, op_bha) on a binary posterior
+        (internal order in, public order out)."""
+        post = np.ascontiguousarray(post, dtype=np.float64)
+        first = self.select(post, n, 1, 1)
+        first_pub = int(sum(1 << (n - 1 - i) for i in range(n) if first >> i & 1))
+        out = np.zeros(max(count, 1), np.uint32)
+        if self.lib.orc_select_experiments(_ptr(post), n, count, first_pub, _ptr(out, _up)) != 0:
+            raise RuntimeError("oracle select_experiments failed")
+        return [int(v) for v in out[:count]]
+
     # drivers ---------------------------------------------------------------
     def session(self, dilution, n, k, pi0, stages, seed, session, true_state, selector=AUTO, alpha=0.99,
                 h=0.005, up=0.01, lo=0.01):
@@ -260,6 +282,7 @@ class Reference:
                                          c_double, c_double, _dp]
         L.ref_session.argtypes = [c_int, c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_double, c_int,
                                   c_uint64, c_uint64, c_uint32, _up, _up, _up, _up, _dp]
+        L.ref_select_experiments.argtypes = [c_int, _dp, c_int, _up, _up, c_int, c_int, _up]
 
     def _check(self, rc):
         if rc != 0:
@@ -268,6 +291,16 @@ class Reference:
     @staticmethod
     def _type(dilution):
         return 4 if dilution else 3
+
+    def select_experiments(self, pi0, updates, count, selector=1):
+        """bgt::Lattice::select_experiments after `updates` [(e, r)] (public order)."""
+        pi0 = np.ascontiguousarray(pi0, dtype=np.float64)
+        e = np.array([u[0] for u in updates] or [0], np.uint32)
+        r = np.array([u[1] for u in updates] or [0], np.uint32)
+        out = np.zeros(max(count, 1), np.uint32)
+        self._check(self.lib.ref_select_experiments(len(pi0), _ptr(pi0), len(updates), _ptr(e, _up), _ptr(r, _up),
+                                                    count, selector, _ptr(out, _up)))
+        return [int(v) for v in out[:count]]
 
     def prior(self, pi0, k=1):
         pi0 = np.ascontiguousarray(pi0, dtype=np.float64)

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <exception>
 #include <memory>
+#include <span>
 #include <vector>
 
 #include "bgt_session_rng.h"
@@ -94,6 +95,22 @@ int ref_dilution_table(int n, double alpha, double h, double *out)
 		for (int row = 0; row < n; row++)
 			for (int col = 0; col <= n; col++)
 				out[row * (n + 1) + col] = col <= row + 1 ? table.rows()[row][col] : 0.0;
+	});
+}
+
+// bgt::Lattice::select_experiments (src/core/lattice_api.cpp:116-168) through
+// the public API: a binary non-dilution lattice from `pi0`, `nupd` updates in
+// public order, then `count` experiments (public order).
+int ref_select_experiments(int n, const double *pi0, int nupd, const uint32_t *upd_e, const uint32_t *upd_r,
+						   int count, int selector, uint32_t *out)
+{
+	return guarded([&] {
+		bgt::Lattice lattice(bgt::LatticeType::replicated_non_dilution, n, std::span<const double>(pi0, n));
+		for (int i = 0; i < nupd; i++)
+			lattice.update(upd_e[i], upd_r[i]);
+		const std::vector<bgt::state_t> got = lattice.select_experiments(count, static_cast<bgt::SelectorType>(selector));
+		for (std::size_t i = 0; i < got.size(); i++)
+			out[i] = got[i];
 	});
 }
 

@@ -153,6 +153,24 @@ int main(int argc, char **argv)
 	expect_equal(lattice.select_experiment(), 3, "auto selection");
 	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bha), 3, "Op-BHA selection");
 	expect_equal(lattice.select_experiment(bgt::SelectorType::op_bbpa), 3, "Op-BBPA selection");
+	{
+		// tests/cpp/unit/lattice_api_test.cpp:75-79
+		const std::vector<bgt::state_t> lookahead = lattice.select_experiments(2, bgt::SelectorType::op_bha);
+		expect_equal(static_cast<long long>(lookahead.size()), 2, "k-lookahead size");
+		expect_equal(lookahead[0], 3, "k-lookahead first experiment");
+		expect_equal(lookahead[1], 2, "k-lookahead second experiment");
+		expect_equal(lattice.select_experiments(1, bgt::SelectorType::op_bbpa)[0], 3, "selector BBPA k=1 experiment");
+		bool threw = false;
+		try
+		{
+			(void)lattice.select_experiments(2, bgt::SelectorType::op_bbpa);
+		}
+		catch (const std::invalid_argument &)
+		{
+			threw = true;
+		}
+		expect_equal(threw, 1, "Op-BBPA lookahead throws std::invalid_argument");
+	}
 	lattice.update(1, 1);
 	const double den = 0.60 * 0.99 + 0.40 * 0.01;
 	expect_near(lattice.posterior_probability(0), 0.08 * 0.01 / den, 1e-12, "posterior state 0");

@@ -178,3 +178,29 @@ def test_test_accuracy_extension(oracle):
         np.testing.assert_array_equal(oracle.run_simulation(0, 4, 1, pi0, 3, branch=1e-4), want)
     with oracle.test_accuracy(0.95, 0.98):
         assert np.max(np.abs(oracle.run_simulation(0, 4, 1, pi0, 3, branch=1e-4) - want)) > 1e-6
+
+
+def _rev(v, n):
+    return int(sum(1 << (n - 1 - i) for i in range(n) if v >> i & 1))
+
+
+def test_lookahead_pin(oracle):
+    # tests/cpp/unit/lattice_api_test.cpp:75-79: select_experiments(2, op_bha) on
+    # the prior {0.2, 0.4} is [3, 2] (public order).
+    assert oracle.select_experiments(oracle.prior([0.2, 0.4]), 2, 2) == [3, 2]
+    assert oracle.select_experiments(oracle.prior([0.2, 0.4]), 2, 1) == [3]
+    assert oracle.select_experiments(oracle.prior([0.2, 0.4]), 2, 0) == []
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference library not built here (oracle/_ref)")
+def test_lookahead_bit_exact_against_reference(oracle):
+    ref = Reference(strict=True)
+    assert ref.select_experiments([0.2, 0.4], [], 2) == [3, 2]
+    rng = np.random.default_rng(31)
+    for n, count in ((3, 3), (5, 3), (7, 3), (8, 4)):
+        pi0 = rng.uniform(0.02, 0.3, n)
+        updates = [(int(rng.integers(1, 1 << n)), int(rng.integers(0, 2))) for _ in range(3)]
+        post = oracle.prior(pi0)
+        for e, r in updates:
+            post = oracle.update(0, n, 1, post, _rev(e, n), r, in_place=True)
+        assert oracle.select_experiments(post, n, count) == ref.select_experiments(pi0, updates, count), (n, updates)
