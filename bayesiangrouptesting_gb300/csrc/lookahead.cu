@@ -90,40 +90,42 @@ __device__ __forceinline__ bool key_less(u64 ahi, u64 alo, unsigned int apub, u6
 // Scores candidates e = 1 .. 2^n - 1 against the previous experiments
 // (their 2^(m-1) intersection masks, masks[0] = every subject); each CTA
 // writes its best (score hi, score lo, public index) to out[3 * blockIdx.x].
-// Group index J (m bits, bit m - 1 = the candidate) of lane l is l * R + r.
+// R > 1 (m > 5): one candidate per warp, group index J = lane * R + r.
+// R = 1 (m <= 5): 32 / 2^m candidates per warp, lane = slot * 2^m + J, so
+// small lookaheads keep every lane busy.
 template <int R>
 __global__ void __launch_bounds__(kScoreThreads) lookahead_score(const u64 *__restrict__ d, int n, int m,
 																  const unsigned int *__restrict__ masks, u64 *out)
 {
 	constexpr int kLogR = R == 1 ? 0 : R == 2 ? 1 : R == 4 ? 2 : R == 8 ? 3 : R == 16 ? 4 : 5;
-	__shared__ u64 s_hi[kScoreWarps], s_lo[kScoreWarps];
-	__shared__ unsigned int s_pub[kScoreWarps];
+	__shared__ u64 s_hi[kScoreThreads], s_lo[kScoreThreads];
+	__shared__ unsigned int s_pub[kScoreThreads];
 	const unsigned int lane = threadIdx.x & 31u;
 	const unsigned int warp = threadIdx.x >> 5;
 	const int groups = 1 << m;
 	const int prev = m - 1;
-	const bool active = static_cast<int>(lane) * R < groups;
+	const int per_warp = R == 1 ? 32 / groups : 1; // candidates per warp
+	const unsigned int slot = R == 1 ? lane >> m : 0u;
+	const unsigned int jbase = R == 1 ? lane & static_cast<unsigned int>(groups - 1) : lane * R;
 	const unsigned int full = n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
 	const u64 z = d[full];
 	u64 best_hi = ~u64{0}, best_lo = ~u64{0};
 	unsigned int best_pub = 0xFFFFFFFFu;
 	const unsigned long long total = 1ull << n;
-	const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * kScoreWarps;
-	for (unsigned long long c = blockIdx.x * static_cast<unsigned long long>(kScoreWarps) + warp + 1; c < total;
-		 c += stride)
+	const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * kScoreWarps * per_warp;
+	for (unsigned long long c0 = (blockIdx.x * static_cast<unsigned long long>(kScoreWarps) + warp) * per_warp + 1;
+		 c0 < total; c0 += stride)
 	{
+		const unsigned long long c = c0 + slot;
+		const bool valid = c < total;
 		const unsigned int e = static_cast<unsigned int>(c);
 		u64 f[R];
 #pragma unroll
 		for (int r = 0; r < R; r++)
 		{
-			f[r] = 0;
-			const int J = static_cast<int>(lane) * R + r;
-			if (active)
-			{
-				const unsigned int x = masks[J & ((1 << prev) - 1)];
-				f[r] = d[(J >> prev) & 1 ? (e & x) : x];
-			}
+			const unsigned int J = jbase + r;
+			const unsigned int x = masks[J & ((1u << prev) - 1u)];
+			f[r] = valid ? d[(J >> prev) & 1u ? (e & x) : x] : 0;
 		}
 		// Superset Moebius transform: mass(g) = sum_{J >= g} (-1)^{|J - g|} S(J).
 #pragma unroll
@@ -146,18 +148,17 @@ __global__ void __launch_bounds__(kScoreThreads) lookahead_score(const u64 *__re
 			}
 		}
 		u128 acc = 0;
-		if (active)
-		{
 #pragma unroll
-			for (int r = 0; r < R; r++)
-			{
-				const u128 scaled = static_cast<u128>(f[r]) << m;
-				acc += scaled >= z ? scaled - z : static_cast<u128>(z) - scaled;
-			}
+		for (int r = 0; r < R; r++)
+		{
+			const u128 scaled = static_cast<u128>(f[r]) << m;
+			acc += scaled >= z ? scaled - z : static_cast<u128>(z) - scaled;
 		}
 		u64 lo = static_cast<u64>(acc), hi = static_cast<u64>(acc >> 64);
-#pragma unroll
-		for (int off = 16; off > 0; off >>= 1)
+		// Sum over the lanes of one candidate: a segment of 2^m lanes (R = 1)
+		// or the whole warp.
+		const int span = R == 1 ? groups : 32;
+		for (int off = span >> 1; off > 0; off >>= 1)
 		{
 			const u64 olo = __shfl_down_sync(0xFFFFFFFFu, lo, off);
 			const u64 ohi = __shfl_down_sync(0xFFFFFFFFu, hi, off);
@@ -166,33 +167,35 @@ __global__ void __launch_bounds__(kScoreThreads) lookahead_score(const u64 *__re
 			lo = sum;
 		}
 		const unsigned int pub = __brev(e) >> (32 - n);
-		if (lane == 0 && key_less(hi, lo, pub, best_hi, best_lo, best_pub))
+		if (valid && (lane & static_cast<unsigned int>(span - 1)) == 0 && key_less(hi, lo, pub, best_hi, best_lo, best_pub))
 		{
 			best_hi = hi;
 			best_lo = lo;
 			best_pub = pub;
 		}
 	}
-	if (lane == 0)
+	s_hi[threadIdx.x] = best_hi;
+	s_lo[threadIdx.x] = best_lo;
+	s_pub[threadIdx.x] = best_pub;
+	for (int off = kScoreThreads / 2; off > 0; off >>= 1)
 	{
-		s_hi[warp] = best_hi;
-		s_lo[warp] = best_lo;
-		s_pub[warp] = best_pub;
+		__syncthreads();
+		if (static_cast<int>(threadIdx.x) < off)
+		{
+			const int o = threadIdx.x + off;
+			if (key_less(s_hi[o], s_lo[o], s_pub[o], s_hi[threadIdx.x], s_lo[threadIdx.x], s_pub[threadIdx.x]))
+			{
+				s_hi[threadIdx.x] = s_hi[o];
+				s_lo[threadIdx.x] = s_lo[o];
+				s_pub[threadIdx.x] = s_pub[o];
+			}
+		}
 	}
-	__syncthreads();
 	if (threadIdx.x == 0)
 	{
-		// Thread 0 still holds warp 0's best.
-		for (int w = 1; w < kScoreWarps; w++)
-			if (key_less(s_hi[w], s_lo[w], s_pub[w], best_hi, best_lo, best_pub))
-			{
-				best_hi = s_hi[w];
-				best_lo = s_lo[w];
-				best_pub = s_pub[w];
-			}
-		out[3 * blockIdx.x] = best_hi;
-		out[3 * blockIdx.x + 1] = best_lo;
-		out[3 * blockIdx.x + 2] = best_pub;
+		out[3 * blockIdx.x] = s_hi[0];
+		out[3 * blockIdx.x + 1] = s_lo[0];
+		out[3 * blockIdx.x + 2] = s_pub[0];
 	}
 }
 
