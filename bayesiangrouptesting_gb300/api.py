@@ -720,6 +720,9 @@ class Lattice:
 
     # -- session -------------------------------------------------------------
     def select_experiment(self, selector: SelectorType = SelectorType.auto_select) -> int:
+        if _resolve_selector(selector, self._variants) == SelectorType.op_bha and self._variants != 1:
+            # std::invalid_argument of src/kernels/cpu/bbpa.cpp:864-867 (ValueError in Python)
+            raise ValueError("Op-BHA experiment selection is only supported for binary lattices.")
         out = ctypes.c_uint32()
         _call(self._lib.bgt_gpu_lattice_select(self._handle, int(selector), ctypes.byref(out)))
         return self._to_public(out.value)

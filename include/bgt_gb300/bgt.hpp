@@ -316,6 +316,9 @@ class Lattice
 	}
 	state_t select_experiment(SelectorType selector = SelectorType::auto_select) const
 	{
+		// Model-level check of Lattice::select_experiment (src/kernels/cpu/bbpa.cpp:864-867).
+		if (selector == SelectorType::op_bha && variants_ != 1)
+			throw std::invalid_argument("Op-BHA experiment selection is only supported for binary lattices.");
 		uint32_t e = 0;
 		detail::check(bgt_gpu_lattice_select(h_, static_cast<int>(selector), &e));
 		return to_internal(e);

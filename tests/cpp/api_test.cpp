@@ -186,8 +186,19 @@ int main(int argc, char **argv)
 	bgt::Lattice multinomial(bgt::LatticeType::replicated_non_dilution, 3, 2, multinomial_prior);
 	expect_equal(multinomial.select_experiment(bgt::SelectorType::op_bbpa), brute_force_bbpa(multinomial, 3, 2),
 				 "multinomial BBPA = brute force");
-	expect_error([&] { multinomial.select_experiment(bgt::SelectorType::op_bha); }, bgt::StatusCode::unsupported,
-				 "Op-BHA with two variants");
+	{
+		// std::invalid_argument, as the reference's model throws (src/kernels/cpu/bbpa.cpp:864-867).
+		bool threw = false;
+		try
+		{
+			(void)multinomial.select_experiment(bgt::SelectorType::op_bha);
+		}
+		catch (const std::invalid_argument &)
+		{
+			threw = true;
+		}
+		expect_equal(threw, 1, "Op-BHA with two variants throws std::invalid_argument");
+	}
 
 	const bgt::DilutionTable table(2, 0.99, 0.005);
 	expect_near(table.at(1, 0), 0.99, 1e-12, "dilution row 1, 0 positives");

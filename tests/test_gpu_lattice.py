@@ -1,5 +1,7 @@
 """Parity of the device lattice (prior, update, selection, classification,
 sessions) against the CPU oracle, through the C ABI."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -121,8 +123,9 @@ def test_multinomial_reference_pin(gpu, oracle):
         if score < best:
             best, best_e = score, e
     assert got == best_e
-    with pytest.raises(bgt.Error):
+    with pytest.raises(ValueError):  # std::invalid_argument in the reference (bbpa.cpp:864-867)
         lat.select_experiment(bgt.SelectorType.op_bha)
+    assert bgt.api.load().bgt_gpu_lattice_select(lat.handle, 1, ctypes.byref(ctypes.c_uint32())) == 2
 
 
 @pytest.mark.parametrize("k,n,dilution", [(2, 3, False), (2, 6, True), (2, 9, False), (2, 12, True), (3, 4, False),
