@@ -20,6 +20,7 @@ import numpy as np
 
 from . import _native
 from ._native import NativeError, TreeStatsC, check, load
+from .logconfig import LogLevel, LogSubsystem, log_message
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _up = ctypes.POINTER(ctypes.c_uint32)
@@ -372,6 +373,13 @@ class SimulationConfig:
     # Extension: a non-dilution likelihood other than the reference's 0.99 / 0.99.
     test_accuracy: Optional[TestAccuracy] = None
 
+    def __setattr__(self, name, value):
+        # The reference's binding converts to std::vector<double>: lists or
+        # numpy arrays are stored as lists of floats.
+        if name in ("prior", "evaluation_prior") and value is not None:
+            value = [float(v) for v in value]
+        super().__setattr__(name, value)
+
 
 @dataclass
 class SimulationResult:
@@ -571,6 +579,9 @@ def run_simulation(config: SimulationConfig) -> SimulationResult:
     if not lib.bgt_cuda_provider_available():
         raise Error(StatusCode.cuda_error, "CUDA provider requested, but no CUDA device is available.")
     progress.maybe_emit("starting CUDA evaluation", force=True)
+    log_message(LogLevel.info, LogSubsystem.runtime,
+                f"local_tree on the CUDA provider: subjects={config.subjects} variants={config.variants} "
+                f"depth={config.options.search_depth}")
     prior = np.ascontiguousarray(config.prior, dtype=np.float64)
     dil = None
     if _uses_dilution(config.lattice_type):

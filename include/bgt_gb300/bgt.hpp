@@ -17,17 +17,21 @@
 #pragma once
 
 #include <atomic>
+#include <cctype>
+#include <cstdlib>
 #include <chrono>
 #include <cstdint>
 #include <filesystem>
 #include <fstream>
 #include <iomanip>
 #include <iostream>
+#include <mutex>
 #include <optional>
 #include <span>
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <string_view>
 #include <utility>
 #include <vector>
 
@@ -970,6 +974,201 @@ class CudaProvider
 						 st.expected_tests};
 	}
 };
+
+// ---- Logging settings (include/bgt/logging.hpp:11-52, behaviour of
+// src/runtime/logging.cpp): a process-wide configuration, the environment
+// variables BGT_LOG_LEVEL / BGT_LOG_SUBSYS / BGT_LOG_FILE / BGT_LOG_RANKS /
+// BGT_LOG_COLOR / BGT_PERF_LEVEL applied on the first read.  This process is
+// one rank, so the rank filter never drops a message.
+enum class LogLevel
+{
+	off = 0,
+	fatal = 1,
+	error = 2,
+	warn = 3,
+	info = 4,
+	debug = 5,
+	trace = 6
+};
+
+enum class LogSubsystem
+{
+	core,
+	model,
+	tree,
+	runtime,
+	parallel,
+	cuda,
+	jit,
+	perf
+};
+
+struct LogConfig
+{
+	LogLevel level = LogLevel::warn;
+	std::vector<LogSubsystem> subsystems;
+	std::vector<int> rank_filter;
+	bool color = false;
+	bool timestamps = true;
+	std::filesystem::path file_path;
+};
+
+inline LogLevel parse_log_level(std::string_view value)
+{
+	std::string v(value);
+	for (char &c : v)
+		c = static_cast<char>(std::tolower(static_cast<unsigned char>(c)));
+	const std::pair<const char *, LogLevel> names[] = {
+		{"off", LogLevel::off},	  {"fatal", LogLevel::fatal}, {"error", LogLevel::error}, {"warn", LogLevel::warn},
+		{"warning", LogLevel::warn}, {"info", LogLevel::info},	  {"debug", LogLevel::debug}, {"trace", LogLevel::trace}};
+	for (const auto &[name, level] : names)
+		if (v == name)
+			return level;
+	return LogLevel::warn;
+}
+
+inline LogSubsystem parse_log_subsystem(std::string_view value)
+{
+	std::string v(value);
+	for (char &c : v)
+		c = static_cast<char>(std::tolower(static_cast<unsigned char>(c)));
+	const char *names[] = {"core", "model", "tree", "runtime", "parallel", "cuda", "jit", "perf"};
+	for (int i = 0; i < 8; i++)
+		if (v == names[i])
+			return static_cast<LogSubsystem>(i);
+	return LogSubsystem::runtime;
+}
+
+inline const char *log_level_name(LogLevel level)
+{
+	const char *names[] = {"OFF", "FATAL", "ERROR", "WARN", "INFO", "DEBUG", "TRACE"};
+	const int i = static_cast<int>(level);
+	return i >= 0 && i < 7 ? names[i] : "UNKNOWN";
+}
+
+inline const char *log_subsystem_name(LogSubsystem subsystem)
+{
+	const char *names[] = {"core", "model", "tree", "runtime", "parallel", "cuda", "jit", "perf"};
+	const int i = static_cast<int>(subsystem);
+	return i >= 0 && i < 8 ? names[i] : "unknown";
+}
+
+namespace detail
+{
+
+struct LogState
+{
+	std::mutex mutex;
+	LogConfig config;
+	bool env_applied = false;
+};
+
+inline LogState &log_state()
+{
+	static LogState state;
+	return state;
+}
+
+inline std::vector<std::string> split_list(const std::string &value)
+{
+	std::vector<std::string> parts;
+	std::string cur;
+	for (char c : value)
+	{
+		if (c == ',')
+		{
+			if (!cur.empty())
+				parts.push_back(cur);
+			cur.clear();
+		}
+		else
+			cur.push_back(c);
+	}
+	if (!cur.empty())
+		parts.push_back(cur);
+	return parts;
+}
+
+// Caller holds the state's mutex.
+inline void apply_log_environment(LogState &st)
+{
+	if (st.env_applied)
+		return;
+	st.env_applied = true;
+	if (const char *v = std::getenv("BGT_LOG_LEVEL"))
+		st.config.level = parse_log_level(v);
+	if (const char *v = std::getenv("BGT_LOG_SUBSYS"))
+	{
+		st.config.subsystems.clear();
+		for (const std::string &p : split_list(v))
+			st.config.subsystems.push_back(parse_log_subsystem(p));
+	}
+	if (const char *v = std::getenv("BGT_LOG_FILE"))
+		st.config.file_path = v;
+	if (const char *v = std::getenv("BGT_LOG_RANKS"))
+	{
+		st.config.rank_filter.clear();
+		for (const std::string &p : split_list(v))
+			st.config.rank_filter.push_back(std::stoi(p));
+	}
+	if (const char *v = std::getenv("BGT_LOG_COLOR"))
+	{
+		const std::string c = v;
+		st.config.color = c == "1" || c == "true" || c == "on" || c == "TRUE" || c == "ON";
+	}
+	if (const char *v = std::getenv("BGT_PERF_LEVEL"))
+	{
+		const LogLevel perf = parse_log_level(v);
+		if (static_cast<int>(perf) > static_cast<int>(st.config.level))
+			st.config.level = perf;
+		bool has = false;
+		for (LogSubsystem s : st.config.subsystems)
+			has = has || s == LogSubsystem::perf;
+		if (!has)
+			st.config.subsystems.push_back(LogSubsystem::perf);
+	}
+}
+
+} // namespace detail
+
+inline void set_log_config(LogConfig config)
+{
+	auto &st = detail::log_state();
+	std::lock_guard<std::mutex> lock(st.mutex);
+	st.config = std::move(config);
+}
+
+inline LogConfig get_log_config()
+{
+	auto &st = detail::log_state();
+	std::lock_guard<std::mutex> lock(st.mutex);
+	detail::apply_log_environment(st);
+	return st.config;
+}
+
+inline void set_log_level(LogLevel level)
+{
+	auto &st = detail::log_state();
+	std::lock_guard<std::mutex> lock(st.mutex);
+	st.config.level = level;
+}
+
+inline bool log_enabled(LogLevel level, LogSubsystem subsystem)
+{
+	auto &st = detail::log_state();
+	std::lock_guard<std::mutex> lock(st.mutex);
+	detail::apply_log_environment(st);
+	if (st.config.level == LogLevel::off || level == LogLevel::off)
+		return false;
+	if (static_cast<int>(level) > static_cast<int>(st.config.level))
+		return false;
+	if (st.config.subsystems.empty())
+		return true;
+	for (LogSubsystem s : st.config.subsystems)
+		if (s == subsystem)
+			return true;
+	return false;
+}
 
 // The CPU provider is always available, as in the reference; this package
 // runs only the device path.

@@ -182,6 +182,28 @@ int main(int argc, char **argv)
 	expect_equal(lattice.negative_classification_mask(), 1, "negative mask");
 	expect_equal(lattice.is_classified(), 0, "not classified");
 
+	{
+		// Logging settings round trip (tests/python/unit/test_public_api.py:36-53 of the reference).
+		bgt::LogConfig config;
+		config.level = bgt::LogLevel::debug;
+		config.subsystems = {bgt::LogSubsystem::runtime};
+		config.rank_filter = {0, 2};
+		config.timestamps = false;
+		bgt::set_log_config(config);
+		const bgt::LogConfig got = bgt::get_log_config();
+		expect_equal(got.level == bgt::LogLevel::debug, 1, "log level round trip");
+		expect_equal(got.subsystems.size() == 1 && got.subsystems[0] == bgt::LogSubsystem::runtime, 1,
+					 "log subsystems round trip");
+		expect_equal(got.rank_filter.size() == 2 && got.rank_filter[1] == 2, 1, "log rank filter round trip");
+		expect_equal(bgt::log_enabled(bgt::LogLevel::info, bgt::LogSubsystem::runtime), 1, "runtime info enabled");
+		expect_equal(bgt::log_enabled(bgt::LogLevel::info, bgt::LogSubsystem::cuda), 0, "cuda filtered out");
+		bgt::set_log_level(bgt::LogLevel::warn);
+		expect_equal(bgt::get_log_config().level == bgt::LogLevel::warn, 1, "set_log_level");
+		expect_equal(bgt::parse_log_level("Warning") == bgt::LogLevel::warn, 1, "parse warning");
+		expect_equal(std::string(bgt::log_level_name(bgt::LogLevel::trace)) == "TRACE", 1, "level name");
+		bgt::set_log_config(bgt::LogConfig{});
+	}
+
 	const std::vector<double> multinomial_prior{0.11, 0.23, 0.31, 0.41, 0.17, 0.29};
 	bgt::Lattice multinomial(bgt::LatticeType::replicated_non_dilution, 3, 2, multinomial_prior);
 	expect_equal(multinomial.select_experiment(bgt::SelectorType::op_bbpa), brute_force_bbpa(multinomial, 3, 2),
