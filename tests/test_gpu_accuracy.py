@@ -107,6 +107,7 @@ def test_device_session(gpu, oracle, n, k, selector):
     (8, 1, 5, 0.0, 0.01),    # leaf sums of the device-built tree
     (8, 1, 5, 1e-4, 0.01),   # the per-true-state sweep with pruning
     (10, 1, 6, 0.0, 0.01),
+    (16, 1, 4, 0.0, 0.01),   # the n=16 search-depth-4 configuration at 0.95 / 0.98
     (5, 1, 17, 0.0, 0.1),    # 2^17 slots: the host-driven level loop (30 leaves)
     (3, 2, 3, 0.0, 0.01),    # multinomial Op-BBPA
     (3, 2, 3, 1e-3, 0.01),
