@@ -950,20 +950,30 @@ class CudaProvider
 {
   public:
 	bool available() const { return cuda_available(); }
+	// `accuracy` (an extension) replaces the non-dilution likelihood.
 	TreeStats run(LatticeType type, int subjects, int variants, std::span<const host_probability_t> prior,
-				  const SimulationOptions &options, const DilutionTable *dilution) const
+				  const SimulationOptions &options, const DilutionTable *dilution,
+				  const TestAccuracy *accuracy = nullptr) const
 	{
 		if (prior.size() != static_cast<std::size_t>(subjects) * static_cast<std::size_t>(variants))
 			throw Error(StatusCode::invalid_argument, "prior length must equal subjects * variants.");
 		const bool dil = detail::uses_dilution(type);
 		if (dil && dilution == nullptr)
 			throw Error(StatusCode::invalid_argument, "dilution table is required for dilution models.");
+		if (dil && accuracy != nullptr)
+			throw Error(StatusCode::invalid_argument, "test accuracy applies to non-dilution models.");
 		bgt_tree_stats st{};
-		detail::check(bgt_cuda_provider_run(dil ? 1 : 0, subjects, variants, prior.data(), options.search_depth,
-											options.threshold_up, options.threshold_lo, options.branch_threshold,
-											static_cast<int>(options.selector),
-											dil ? const_cast<host_probability_t **>(dilution->rows()) : nullptr,
-											&st));
+		if (accuracy != nullptr)
+			detail::check(bgt_gpu_tree_run_accuracy(subjects, variants, prior.data(), options.search_depth,
+													options.threshold_up, options.threshold_lo,
+													options.branch_threshold, static_cast<int>(options.selector),
+													accuracy->sensitivity, accuracy->specificity, &st));
+		else
+			detail::check(bgt_cuda_provider_run(dil ? 1 : 0, subjects, variants, prior.data(), options.search_depth,
+												options.threshold_up, options.threshold_lo, options.branch_threshold,
+												static_cast<int>(options.selector),
+												dil ? const_cast<host_probability_t **>(dilution->rows()) : nullptr,
+												&st));
 		return TreeStats{st.total_leaves,
 						 st.correct_probability,
 						 st.incorrect_probability,
