@@ -70,7 +70,9 @@ def test_argument_errors(gpu):
 
 
 @pytest.mark.parametrize("n,count,dilution", [(3, 3, False), (6, 4, False), (9, 3, True), (11, 3, False),
-                                              (12, 2, True)])
+                                              (12, 2, True),
+                                              # 6..10 experiments: 2..32 response groups per lane
+                                              (6, 10, False), (8, 8, True), (10, 7, False)])
 def test_matches_oracle(gpu, oracle, n, count, dilution):
     rng = np.random.default_rng(900 + n)
     pi0 = rng.uniform(0.02, 0.3, n)
