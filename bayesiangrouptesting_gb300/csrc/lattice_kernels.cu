@@ -776,8 +776,7 @@ __device__ __forceinline__ void load_class_table(const LatticeDev &L, unsigned i
 			rest /= radix;
 			// Non-dilution class c = contained (1) or not (0); dilution class = popcount(e & s_v).
 			const int pc = L.dilution ? c : (c ? pool : (pool > 0 ? pool - 1 : 0));
-			f *= binary_likelihood(L.dilution, pool, pc, (L.pend_r >> v) & 1u, L.dil, L.orig_n + 1, specificity_of(L),
-								   sensitivity_of(L));
+			f *= binary_likelihood(L, pool, pc, (L.pend_r >> v) & 1u);
 		}
 		if (L.fp32)
 			reinterpret_cast<float *>(g_ctab)[idx] = static_cast<float>(f / z);
@@ -801,9 +800,7 @@ __device__ __forceinline__ void fill_lattice_cache(const LatticeDev &L, int li, 
 		if (with_ctab && mode == kUpdate && k == 1)
 		{
 			ps.ctab[tid] = static_cast<int>(tid) <= pool
-							   ? binary_likelihood(L.dilution, pool, tid, L.pend_r, L.dil, L.orig_n + 1,
-												   specificity_of(L), sensitivity_of(L)) /
-									 L.z_norm
+							   ? binary_likelihood(L, pool, tid, L.pend_r) / L.z_norm
 							   : 0.0;
 			ps.ctab32[tid] = static_cast<float>(ps.ctab[tid]);
 		}

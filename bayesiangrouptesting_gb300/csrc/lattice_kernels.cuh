@@ -420,6 +420,15 @@ __device__ __forceinline__ double binary_likelihood(int dilution, int pool, int 
 	return (r & 1u) != 0 ? p : 1.0 - p;
 }
 
+// The same for lattice L's own model; the accuracy fields are read only on
+// the non-dilution branch (they would otherwise stay live in the callers).
+__device__ __forceinline__ double binary_likelihood(const LatticeDev &L, int pool, int pc, unsigned int r)
+{
+	if (!L.dilution)
+		return binary_likelihood(0, pool, pc, r, nullptr, 0, specificity_of(L), sensitivity_of(L));
+	return binary_likelihood(1, pool, pc, r, L.dil, L.orig_n + 1, 0.0, 0.0);
+}
+
 __device__ __forceinline__ bool better(unsigned long long s, unsigned int e, unsigned long long bs, unsigned int be)
 {
 	return s < bs || (s == bs && e < be);
