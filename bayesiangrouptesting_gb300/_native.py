@@ -58,6 +58,9 @@ class ServeRequestC(ctypes.Structure):
         ("seed", c_uint64),
         ("session", c_uint64),
         ("true_state", c_uint32),
+        ("test_accuracy", c_int),
+        ("sensitivity", c_double),
+        ("specificity", c_double),
     ]
 
 

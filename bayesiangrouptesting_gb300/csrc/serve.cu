@@ -373,6 +373,8 @@ struct bgt_gpu_server
 			h.seed = rq.seed;
 			h.session = rq.session;
 			h.truth = rq.true_state;
+			if (rq.test_accuracy)
+				apply_accuracy(h, TestAccuracy{1, rq.specificity, rq.sensitivity});
 			const size_t S = static_cast<size_t>(cfg.max_stages);
 			unsigned int *o = out_dev + static_cast<size_t>(slot) * 4 * S;
 			h.out_e = o;
@@ -560,6 +562,13 @@ int bgt_gpu_server_submit(bgt_gpu_server *server, const bgt_serve_request *reque
 	if (request->selector < 0 || request->selector > 2)
 	{
 		set_error("unsupported selector");
+		return BGT_GPU_UNSUPPORTED;
+	}
+	if (request->test_accuracy != 0 &&
+		(request->test_accuracy != 1 || request->dilution != 0 ||
+		 !valid_accuracy(request->sensitivity, request->specificity)))
+	{
+		set_error("test accuracy is 0 or 1, for non-dilution sessions, with values in [0, 1]");
 		return BGT_GPU_UNSUPPORTED;
 	}
 	const LatticeGeometry g = tuned_geometry(request->subjects, 1, kServeBatch);

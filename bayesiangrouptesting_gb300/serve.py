@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass
-from typing import List, Optional
+from typing import List, Optional, Tuple
 
 import numpy as np
 
@@ -36,6 +36,8 @@ class SessionRequest:
     alpha: float = 0.99
     h: float = 0.005
     selector: int = 0  # 0 auto (Op-BHA), 1 Op-BHA, 2 Op-BBPA
+    # non-dilution (sensitivity, specificity); None = the reference's 0.99 / 0.99
+    test_accuracy: Optional[Tuple[float, float]] = None
 
 
 @dataclass
@@ -91,8 +93,10 @@ class Server:
         prior = np.ascontiguousarray(req.prior, dtype=np.float64)
         if prior.size != req.subjects:
             raise ValueError("prior length must equal subjects")
+        acc = req.test_accuracy
         c = ServeRequestC(1 if req.dilution else 0, req.subjects, prior.ctypes.data_as(_dp), req.alpha, req.h,
-                          req.selector, req.seed, req.session, req.true_state)
+                          req.selector, req.seed, req.session, req.true_state, 0 if acc is None else 1,
+                          0.0 if acc is None else float(acc[0]), 0.0 if acc is None else float(acc[1]))
         ticket = ctypes.c_uint64()
         _call(self._lib.bgt_gpu_server_submit(self._handle, ctypes.byref(c), ctypes.byref(ticket)))
         return int(ticket.value)

@@ -51,6 +51,12 @@ typedef struct bgt_serve_request
 	int selector;        /* 0 auto (Op-BHA), 1 Op-BHA, 2 Op-BBPA */
 	uint64_t seed, session;
 	uint32_t true_state; /* internal subject order */
+	/* Non-dilution test accuracy (an extension; see
+	 * bgt_gpu_lattice_set_test_accuracy): 0 = the reference's 0.99 / 0.99,
+	 * 1 = sensitivity / specificity below.  Zero-initialised requests keep
+	 * the reference model. */
+	int test_accuracy;
+	double sensitivity, specificity;
 } bgt_serve_request;
 
 typedef struct bgt_serve_result

@@ -147,3 +147,36 @@ def test_fp32_served_sessions_equal_fp32_plain_loop(gpu):
         np.testing.assert_array_equal(plain["experiments"], r.experiments)
         np.testing.assert_array_equal(plain["pos"], r.pos_masks)
         np.testing.assert_array_equal(plain["neg"], r.neg_masks)
+
+
+def test_served_sessions_with_test_accuracy(gpu, oracle):
+    # Non-dilution sessions at sensitivity 0.95 / specificity 0.98 beside
+    # reference-model ones in the same rounds: each equals the oracle's
+    # session under its own model.
+    rng = np.random.default_rng(88)
+    reqs = []
+    for i in range(10):
+        n = int(rng.integers(4, 12))
+        pi0 = rng.uniform(0.01, 0.15, n)
+        truth = int(sum(1 << j for j in range(n) if rng.random() >= pi0[j]))
+        acc = (0.95, 0.98) if i % 2 == 0 else None
+        reqs.append(SessionRequest(n, pi0, truth, seed=5, session=i, test_accuracy=acc))
+    got = serve_all(reqs, memory_budget=GB)
+    for q, r in zip(reqs, got):
+        if q.test_accuracy is not None:
+            with oracle.test_accuracy(*q.test_accuracy):
+                want = oracle.session(0, q.subjects, 1, q.prior, MAX_STAGES, q.seed, q.session, q.true_state,
+                                      selector=0)
+        else:
+            want = oracle.session(0, q.subjects, 1, q.prior, MAX_STAGES, q.seed, q.session, q.true_state, selector=0)
+        stop = _settled_prefix(q.subjects, want["pos"], want["neg"], MAX_STAGES)
+        assert r.error == 0 and r.stages == stop
+        np.testing.assert_array_equal(r.experiments, want["experiments"][:stop])
+        np.testing.assert_array_equal(r.responses, want["responses"][:stop])
+        np.testing.assert_array_equal(r.neg_masks, want["neg"][:stop])
+    # a dilution session cannot take a test accuracy
+    bad = SessionRequest(4, np.full(4, 0.1), 15, seed=1, session=0, dilution=True, alpha=0.01,
+                         test_accuracy=(0.95, 0.98))
+    with Server(GB, max_sessions=4, max_stages=MAX_STAGES) as srv:
+        with pytest.raises(bgt.Error):
+            srv.submit(bad)
