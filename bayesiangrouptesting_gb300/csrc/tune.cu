@@ -12,12 +12,19 @@
 // winner for the process.  W never changes results: the zeta sums are exact
 // integers whatever the blocking.  BGT_GB300_TUNE=0 skips the timing and
 // uses the heuristic (narrow for one lattice, full tiles for batches).
+// BGT_GB300_TUNE_CACHE names a file that keeps the winners across processes:
+// one line "<device>|<SMs>|<atoms>|<batch class> <W>" per timing, read once
+// per process; lines of other devices, malformed lines and widths the split
+// no longer allows are ignored (those pairs are timed again).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
+#include <sstream>
+#include <string>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -37,6 +44,66 @@ std::mutex g_tune_mutex;
 std::map<std::pair<int, int>, int> g_tuned; // (atoms, batch class) -> W
 
 int batch_class(int batch) { return batch <= 1 ? 1 : (batch <= 16 ? 16 : 256); }
+
+// ---- the on-disk cache (caller holds g_tune_mutex) ----
+bool g_disk_loaded = false;
+std::map<std::pair<int, int>, int> g_disk; // this device's stored widths
+
+const char *cache_path()
+{
+	const char *v = std::getenv("BGT_GB300_TUNE_CACHE");
+	return v && v[0] ? v : nullptr;
+}
+
+// "<device name>|<SM count>" with the name's separators replaced.
+std::string device_tag()
+{
+	int dev = 0;
+	cudaDeviceProp prop{};
+	if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return "unknown|0";
+	}
+	std::string name = prop.name;
+	for (char &c : name)
+		if (c == '|' || c == ' ' || c == '\n' || c == '\t')
+			c = '_';
+	return name + "|" + std::to_string(prop.multiProcessorCount);
+}
+
+void load_disk_cache()
+{
+	if (g_disk_loaded)
+		return;
+	g_disk_loaded = true;
+	const char *path = cache_path();
+	if (!path)
+		return;
+	std::ifstream in(path);
+	const std::string tag = device_tag() + "|";
+	std::string line;
+	while (std::getline(in, line))
+	{
+		if (line.compare(0, tag.size(), tag) != 0)
+			continue;
+		std::istringstream rest(line.substr(tag.size()));
+		int atoms = 0, cls = 0, w = 0;
+		char bar = 0;
+		if (!(rest >> atoms >> bar >> cls >> w) || bar != '|' || atoms <= 0 || w <= 0)
+			continue;
+		g_disk.emplace(std::make_pair(atoms, cls), w); // the first line of a pair wins
+	}
+}
+
+void store_disk_cache(int atoms, int cls, int w)
+{
+	const char *path = cache_path();
+	if (!path)
+		return;
+	std::ofstream out(path, std::ios::app);
+	out << device_tag() << '|' << atoms << '|' << cls << ' ' << w << '\n';
+}
 
 bool tuning_enabled()
 {
@@ -184,6 +251,13 @@ LatticeGeometry tuned_geometry(int n, int k, int batch)
 	auto it = g_tuned.find(key);
 	if (it == g_tuned.end())
 	{
+		load_disk_cache();
+		auto stored = g_disk.find(key);
+		if (stored != g_disk.end() && std::find(widths.begin(), widths.end(), stored->second) != widths.end())
+			it = g_tuned.emplace(key, stored->second).first;
+	}
+	if (it == g_tuned.end())
+	{
 		// Scratch lattices: the batch class, at most 2 GB of posterior +
 		// partial sums.
 		const size_t per = (size_t{16} << narrow.atoms) + (size_t{1} << 16);
@@ -203,6 +277,7 @@ LatticeGeometry tuned_geometry(int n, int k, int batch)
 			}
 		}
 		it = g_tuned.emplace(key, best_w).first;
+		store_disk_cache(key.first, key.second, best_w);
 	}
 	return make_geometry(n, k, it->second);
 }

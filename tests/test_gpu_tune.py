@@ -47,3 +47,34 @@ def test_tuned_widths_do_not_change_served_sessions(gpu, monkeypatch):
         assert x.stages == y.stages
         np.testing.assert_array_equal(x.experiments, y.experiments)
         np.testing.assert_array_equal(x.neg_masks, y.neg_masks)
+
+
+_PROBE = (
+    "import bayesiangrouptesting_gb300 as bgt, bayesiangrouptesting_gb300._native as nat\n"
+    "lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 14, [0.05] * 14)\n"
+    "print(nat.launches())\n"
+)
+
+
+def _launches_with_cache(path):
+    import subprocess
+    import sys
+    env = dict(os.environ, BGT_GB300_TUNE="1", BGT_GB300_TUNE_CACHE=str(path))
+    out = subprocess.run([sys.executable, "-c", _PROBE], env=env, capture_output=True, text=True,
+                         cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))), timeout=300)
+    assert out.returncode == 0, out.stderr
+    return int(out.stdout.strip().splitlines()[-1])
+
+
+def test_tuned_widths_persist_across_processes(gpu, tmp_path):
+    cache = tmp_path / "tune.txt"
+    cache.write_text("malformed line\nother-device|1|14|1 64\n")
+    cold = _launches_with_cache(cache)      # times the widths, appends the winner
+    lines = [l for l in cache.read_text().splitlines() if "|14|1 " in l and not l.startswith("other-device")]
+    assert len(lines) == 1
+    warm = _launches_with_cache(cache)      # reads it back: no timing launches
+    assert warm < cold
+    assert len([l for l in cache.read_text().splitlines() if "|14|1 " in l]) == 2  # nothing appended
+    # a width the split does not allow is ignored and timed again
+    cache.write_text(lines[0].rsplit(" ", 1)[0] + " 3\n")
+    assert _launches_with_cache(cache) == cold
