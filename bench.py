@@ -109,6 +109,30 @@ def _dist():
     return world, rank, local
 
 
+def rank_session(rank: int, k: int) -> int:
+    """Session id of step k on a rank: replicas run disjoint session streams."""
+    return (rank << 32) + k
+
+
+def max_over_ranks(values, world: int, device=None):
+    """Each of `values` maximised over the ranks (the slowest rank ends the
+    job); unchanged on one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_throughput(units_per_rank: float, world: int, seconds: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed
+    `units_per_rank` units, the job taking `seconds` (the max over ranks)."""
+    return units_per_rank * world / seconds
+
+
 # -------------------------------------------------- clocks sampling
 class ClockSampler:
     def __init__(self, index: int):
@@ -566,14 +590,14 @@ def run_gpu(args, world, rank, local):
     prior_h = torch.empty(SUBJECTS, dtype=torch.float64, pin_memory=True)
     outs = [torch.empty(STAGES, dtype=torch.int32, pin_memory=True) for _ in range(4)]
     handle = ctypes.c_void_p()
-    first = session_prior(SEED, rank << 32)
+    first = session_prior(SEED, rank_session(rank, 0))
     prior_h.copy_(torch.from_numpy(first))
     _native.check(lib.bgt_gpu_lattice_create(1, SUBJECTS, 1, ctypes.cast(prior_h.data_ptr(), dp), 0,
                                              ctypes.byref(handle)))
     _native.check(lib.bgt_gpu_lattice_set_stream(handle, ctypes.c_void_p(stream.cuda_stream)))
 
     def step(k: int):
-        session = (rank << 32) + k
+        session = rank_session(rank, k)
         pi0 = session_prior(SEED, session)
         truth = session_truth(SEED, session, pi0)
         prior_h.copy_(torch.from_numpy(pi0))
@@ -613,13 +637,10 @@ def run_gpu(args, world, rank, local):
     _native.check(lib.bgt_gpu_profile_read(kl, kms))
     elapsed_ms = start.elapsed_time(end)
     wall_ms = 1e3 * sum(wall_steps)
-    if world > 1:
-        t = torch.tensor([elapsed_ms, wall_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms, wall_ms = float(t[0]), float(t[1])
+    elapsed_ms, wall_ms = max_over_ranks([elapsed_ms, wall_ms], world, device="cuda")
     total_stages = STAGES * args.steps * world
-    value = total_stages / (elapsed_ms / 1e3)
-    e2e = total_stages / (wall_ms / 1e3)
+    value = replica_throughput(STAGES * args.steps, world, elapsed_ms / 1e3)
+    e2e = replica_throughput(STAGES * args.steps, world, wall_ms / 1e3)
 
     n_states = 1 << SUBJECTS
     # Dominant kernel: the update + low-bit zeta pass.  Algorithmic bytes per
