@@ -115,6 +115,8 @@ SIGNATURES = {
     "bgt_gpu_server_session_bytes": ([c_void_p, c_int, POINTER(c_uint64)], c_int),
     "bgt_gpu_lattice_reset": ([c_void_p, _dp], c_int),
     "bgt_gpu_selftest_bounded_wait": ([c_uint32, POINTER(c_int)], c_int),
+    "bgt_gpu_set_memory_limit": ([c_uint64], c_int),
+    "bgt_gpu_memory_in_use": ([POINTER(c_uint64)], c_int),
     "bgt_gpu_lattice_select_experiments": ([c_void_p, c_int, c_int, _up], c_int),
     "bgt_gpu_lattice_set_test_accuracy": ([c_void_p, c_double, c_double], c_int),
     "bgt_gpu_tree_run_accuracy": ([c_int, c_int, _dp, c_int, c_double, c_double, c_double, c_int, c_double, c_double,

@@ -809,6 +809,20 @@ class Lattice:
         return dict(experiments=ex[:n], responses=rs[:n], pos=pm[:n], neg=nm[:n], stages=n)
 
 
+def set_memory_limit(limit_bytes: int) -> None:
+    """Device-memory budget of lattice handles (bgt_gpu_set_memory_limit):
+    an allocation past it raises Error before the device is asked; 0 removes
+    the limit."""
+    _call(load().bgt_gpu_set_memory_limit(int(limit_bytes)))
+
+
+def memory_in_use() -> int:
+    """Device bytes the lattice handles hold (bgt_gpu_memory_in_use)."""
+    out = ctypes.c_uint64()
+    _call(load().bgt_gpu_memory_in_use(ctypes.byref(out)))
+    return int(out.value)
+
+
 def select_experiment(lattice: Lattice, selector: SelectorType = SelectorType.auto_select) -> int:
     return lattice.select_experiment(selector)
 

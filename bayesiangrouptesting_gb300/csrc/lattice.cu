@@ -379,6 +379,18 @@ using namespace bgt_gpu;
 
 // ---------------------------------------------------------------- lattice
 
+namespace
+{
+
+// Device-memory budget of lattice handles (bgt_gpu_set_memory_limit): 0 = no
+// limit.  An allocation that would pass the limit fails the way a failed
+// cudaMalloc does (status 4), before the device is asked, so the failure path
+// can be exercised on a shared GPU without exhausting its memory.
+std::atomic<unsigned long long> g_lattice_limit{0};
+std::atomic<unsigned long long> g_lattice_bytes{0};
+
+} // namespace
+
 struct bgt_gpu_lattice
 {
 	LatticeGeometry g;
@@ -414,8 +426,42 @@ struct bgt_gpu_lattice
 	bool update_pending = false;
 	uint32_t pos = 0, neg = 0;
 
+	unsigned long long owned_bytes = 0; // allocated through alloc(), counted against the budget
+
+	// cudaMalloc of `bytes` into *p under the lattice budget.
+	template <typename T>
+	void alloc(T **p, size_t bytes, const char *what)
+	{
+		const unsigned long long limit = g_lattice_limit.load();
+		const unsigned long long before = g_lattice_bytes.fetch_add(bytes);
+		if (limit != 0 && before + bytes > limit)
+		{
+			g_lattice_bytes.fetch_sub(bytes);
+			throw CudaFailure(std::string(what) + ": device memory budget exceeded");
+		}
+		const cudaError_t err = cudaMalloc(reinterpret_cast<void **>(p), bytes);
+		if (err != cudaSuccess)
+		{
+			g_lattice_bytes.fetch_sub(bytes);
+			*p = nullptr;
+			cuda_check(err, what);
+		}
+		owned_bytes += bytes;
+	}
+
+	// cudaFree of a buffer of `bytes` taken by alloc().
+	void release(void *p, size_t bytes)
+	{
+		if (!p)
+			return;
+		cudaFree(p);
+		owned_bytes -= bytes;
+		g_lattice_bytes.fetch_sub(bytes);
+	}
+
 	~bgt_gpu_lattice()
 	{
+		g_lattice_bytes.fetch_sub(owned_bytes);
 		cudaFree(dev);
 		cudaFree(q);
 		cudaFree(m1);
@@ -643,27 +689,27 @@ int bgt_gpu_lattice_create(int lattice_type, int subjects, int variants, const d
 			lat->stream = lat->own_stream;
 			const size_t states = size_t{1} << g.atoms;
 			const size_t rows = size_t{1} << g.hbits;
-			cuda_check(cudaMalloc(&lat->dev, sizeof(LatticeDev)), "alloc state");
+			lat->alloc(&lat->dev, sizeof(LatticeDev), "alloc state");
 			const size_t esize = precision == BGT_GPU_FP32 ? sizeof(float) : sizeof(double);
-			cuda_check(cudaMalloc(&lat->q, states * esize), "alloc posterior");
-			cuda_check(cudaMalloc(&lat->m1, static_cast<size_t>(g.nblk) * rows * g.colw * sizeof(unsigned long long)),
+			lat->alloc(&lat->q, states * esize, "alloc posterior");
+			lat->alloc(&lat->m1, static_cast<size_t>(g.nblk) * rows * g.colw * sizeof(unsigned long long),
 					   "alloc zeta partials");
-			cuda_check(cudaMalloc(&lat->tile_total, rows * sizeof(unsigned long long)), "alloc tile totals");
-			cuda_check(cudaMalloc(&lat->tile_scale, rows * sizeof(int)), "alloc tile scales");
-			cuda_check(cudaMalloc(&lat->blk_score, (static_cast<size_t>(g.nblk) << g.mbits) * sizeof(unsigned long long)),
+			lat->alloc(&lat->tile_total, rows * sizeof(unsigned long long), "alloc tile totals");
+			lat->alloc(&lat->tile_scale, rows * sizeof(int), "alloc tile scales");
+			lat->alloc(&lat->blk_score, (static_cast<size_t>(g.nblk) << g.mbits) * sizeof(unsigned long long),
 					   "alloc block scores");
-			cuda_check(cudaMalloc(&lat->blk_e, (static_cast<size_t>(g.nblk) << g.mbits) * sizeof(unsigned int)),
+			lat->alloc(&lat->blk_e, (static_cast<size_t>(g.nblk) << g.mbits) * sizeof(unsigned int),
 					   "alloc block winners");
 			if (g.mbits > 0)
-				cuda_check(cudaMalloc(&lat->m2, states * sizeof(unsigned long long)), "alloc middle-pass partials");
-			cuda_check(cudaMalloc(&lat->dil, static_cast<size_t>(subjects) * (subjects + 1) * sizeof(double)),
+				lat->alloc(&lat->m2, states * sizeof(unsigned long long), "alloc middle-pass partials");
+			lat->alloc(&lat->dil, static_cast<size_t>(subjects) * (subjects + 1) * sizeof(double),
 					   "alloc dilution");
-			cuda_check(cudaMalloc(&lat->prior_lo, (size_t{1} << g.tbits) * sizeof(double)), "alloc prior lo");
-			cuda_check(cudaMalloc(&lat->prior_hi, rows * sizeof(double)), "alloc prior hi");
-			cuda_check(cudaMalloc(&lat->pi0, g.atoms * sizeof(double)), "alloc pi0");
-			cuda_check(cudaMalloc(&lat->scratch_u64, 64 * sizeof(unsigned long long)), "alloc scratch");
+			lat->alloc(&lat->prior_lo, (size_t{1} << g.tbits) * sizeof(double), "alloc prior lo");
+			lat->alloc(&lat->prior_hi, rows * sizeof(double), "alloc prior hi");
+			lat->alloc(&lat->pi0, g.atoms * sizeof(double), "alloc pi0");
+			lat->alloc(&lat->scratch_u64, 64 * sizeof(unsigned long long), "alloc scratch");
 			if (variants > 1)
-				cuda_check(cudaMalloc(&lat->ftab, (size_t{1} << (subjects + variants)) * sizeof(unsigned long long)),
+				lat->alloc(&lat->ftab, (size_t{1} << (subjects + variants)) * sizeof(unsigned long long),
 						   "alloc feature masses");
 			cuda_check(cudaMemcpyAsync(lat->pi0, prior, g.atoms * sizeof(double), cudaMemcpyHostToDevice, lat->stream),
 					   "prior upload");
@@ -1095,14 +1141,28 @@ int bgt_gpu_lattice_select_experiments(bgt_gpu_lattice *lattice, int count, int 
 		const size_t states = size_t{1} << n;
 		if (!lattice->la_d)
 		{
-			lattice->la_blocks = lookahead_score_blocks(n);
-			cuda_check(cudaMalloc(&lattice->la_d, states * sizeof(unsigned long long)), "alloc lookahead sums");
-			cuda_check(cudaMalloc(&lattice->la_scratch, 3 * static_cast<size_t>(lattice->la_blocks) *
-															 sizeof(unsigned long long)),
-					   "alloc lookahead scratch");
-			cuda_check(cudaMalloc(&lattice->la_masks, (size_t{1} << (kLookaheadMax - 1)) * sizeof(unsigned int)),
-					   "alloc lookahead masks");
-			cuda_check(cudaMalloc(&lattice->la_result, sizeof(unsigned int)), "alloc lookahead result");
+			// All four or none: la_d, allocated last, marks the set complete.
+			const int blocks = lookahead_score_blocks(n);
+			const size_t scratch_bytes = 3 * static_cast<size_t>(blocks) * sizeof(unsigned long long);
+			const size_t mask_bytes = (size_t{1} << (kLookaheadMax - 1)) * sizeof(unsigned int);
+			try
+			{
+				lattice->alloc(&lattice->la_scratch, scratch_bytes, "alloc lookahead scratch");
+				lattice->alloc(&lattice->la_masks, mask_bytes, "alloc lookahead masks");
+				lattice->alloc(&lattice->la_result, sizeof(unsigned int), "alloc lookahead result");
+				lattice->alloc(&lattice->la_d, states * sizeof(unsigned long long), "alloc lookahead sums");
+			}
+			catch (...)
+			{
+				lattice->release(lattice->la_scratch, scratch_bytes);
+				lattice->release(lattice->la_masks, mask_bytes);
+				lattice->release(lattice->la_result, sizeof(unsigned int));
+				lattice->la_scratch = nullptr;
+				lattice->la_masks = nullptr;
+				lattice->la_result = nullptr;
+				throw;
+			}
+			lattice->la_blocks = blocks;
 		}
 		if (lattice->update_pending || lattice->k1_pending)
 			lattice->run_k1();
@@ -1135,6 +1195,23 @@ int bgt_gpu_lattice_select_experiments(bgt_gpu_lattice *lattice, int count, int 
 		}
 		return BGT_GPU_OK;
 	});
+}
+
+int bgt_gpu_set_memory_limit(uint64_t bytes)
+{
+	g_lattice_limit.store(bytes);
+	return BGT_GPU_OK;
+}
+
+int bgt_gpu_memory_in_use(uint64_t *bytes)
+{
+	if (!bytes)
+	{
+		set_error("null output pointer");
+		return BGT_GPU_MISSING_DILUTION;
+	}
+	*bytes = g_lattice_bytes.load();
+	return BGT_GPU_OK;
 }
 
 int bgt_gpu_lattice_set_test_accuracy(bgt_gpu_lattice *lattice, double sensitivity, double specificity)
@@ -1225,10 +1302,11 @@ int session_run_impl(bgt_gpu_lattice *lattice, int selector, int stages, double 
 			return BGT_GPU_OK;
 		if (stages > lattice->sess_capacity)
 		{
-			cudaFree(lattice->sess_out);
+			lattice->release(lattice->sess_out, 4 * static_cast<size_t>(lattice->sess_capacity) * sizeof(unsigned int));
 			lattice->sess_out = nullptr;
-			cuda_check(cudaMalloc(&lattice->sess_out, 4 * static_cast<size_t>(stages) * sizeof(unsigned int)),
-					   "alloc session outputs");
+			lattice->sess_capacity = 0;
+			lattice->alloc(&lattice->sess_out, 4 * static_cast<size_t>(stages) * sizeof(unsigned int),
+						   "alloc session outputs");
 			lattice->sess_capacity = stages;
 		}
 		if (lattice->dilution)

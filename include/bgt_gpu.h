@@ -163,6 +163,15 @@ BGT_GPU_API int bgt_gpu_lattice_upset_mass(bgt_gpu_lattice *lattice, uint32_t ex
 BGT_GPU_API int bgt_gpu_lattice_response_probability(bgt_gpu_lattice *lattice, uint32_t experiment, uint32_t response,
 													 uint32_t true_state, double **dilution, double *out);
 
+/* Device-memory budget of lattice handles, for callers that share the GPU
+ * and for fault-injection tests: once set (bytes > 0), a lattice allocation
+ * (create, lookahead scratch, session outputs) that would take the lattices'
+ * total above it fails with status 4, "device memory budget exceeded",
+ * before the device is asked; 0 removes the limit.  Servers and trees have
+ * their own budgets.  bgt_gpu_memory_in_use reports the lattices' total. */
+BGT_GPU_API int bgt_gpu_set_memory_limit(uint64_t bytes);
+BGT_GPU_API int bgt_gpu_memory_in_use(uint64_t *bytes);
+
 /* Lattice::select_experiments (include/bgt/lattice.hpp:54;
  * src/core/lattice_api.cpp:116-168): `count` experiments into `experiments`
  * (internal bit order).  Op-BHA (selector 1, or 0 on a binary lattice): the

@@ -117,3 +117,32 @@ def test_bounded_wait_gives_up_and_device_stays_usable(gpu):
     assert time.perf_counter() - t0 < 5.0
     lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 6, np.full(6, 0.1))
     assert 0 <= lat.select_experiment() < 64  # the context still runs kernels
+
+
+def test_memory_budget_fails_allocations_on_the_host(gpu):
+    # Allocation failure injected through the lattice budget: the device is
+    # never asked for more than it has, the failed calls release what they
+    # took, and the lattices that exist keep working.
+    import gc
+    gc.collect()
+    base = bgt.memory_in_use()
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 16, [0.05] * 16)
+    used = bgt.memory_in_use()
+    assert used > base + (1 << 20)  # at least the 2^16 posterior and partial sums
+    bgt.set_memory_limit(used + (1 << 16))
+    try:
+        with pytest.raises(bgt.Error, match="budget"):
+            bgt.Lattice(bgt.LatticeType.replicated_non_dilution, 20, [0.05] * 20)
+        assert bgt.memory_in_use() == used
+        with pytest.raises(bgt.Error, match="budget"):
+            lat.select_experiments(2)  # the lookahead scratch does not fit
+        assert bgt.memory_in_use() == used
+        lat.update(3, 1)
+        assert lat.select_experiment() > 0
+    finally:
+        bgt.set_memory_limit(0)
+    assert len(lat.select_experiments(2)) == 2  # allocates now
+    assert bgt.memory_in_use() > used
+    del lat
+    gc.collect()
+    assert bgt.memory_in_use() == base
