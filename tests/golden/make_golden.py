@@ -80,6 +80,14 @@ def main():
                                    pos=res["pos"].tolist(), neg=res["neg"].tolist(),
                                    posterior_sum=float(np.sum(res["posterior"])),
                                    posterior_head=res["posterior"][:16].tolist()))
+    # k-lookahead (bgt::Lattice::select_experiments, public order) after
+    # seeded updates, through the reference's public API.
+    out["lookahead"] = []
+    for (n, count) in ((2, 2), (4, 3), (6, 4), (7, 3), (9, 3), (5, 6)):
+        pi0 = rng.uniform(0.02, 0.3, n)
+        updates = [(int(rng.integers(1, 1 << n)), int(rng.integers(0, 2))) for _ in range(2)]
+        got = ref.select_experiments(pi0, updates, count)
+        out["lookahead"].append(dict(n=n, pi0=pi0.tolist(), updates=updates, count=count, experiments=got))
     path = os.path.join(HERE, "reference_vectors.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=0)

@@ -121,3 +121,23 @@ def test_n20_against_sampled_candidates(gpu):
         for cand in rng.integers(1, 1 << n, 64):
             other = _score(post_pub, n, got[:step] + [int(cand)])
             assert best <= other + 1e-12, (step, got, int(cand), best, other)
+
+
+def _golden():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_vectors.json")
+    return json.load(open(path)).get("lookahead", [])
+
+
+@pytest.mark.parametrize("case", range(len(_golden())))
+def test_golden_reference_outputs(gpu, oracle, case):
+    # The reference library's own select_experiments outputs (public order).
+    c = _golden()[case]
+    n = c["n"]
+    lat = bgt.Lattice(bgt.LatticeType.replicated_non_dilution, n, c["pi0"])
+    post = oracle.prior(c["pi0"])
+    for e, r in c["updates"]:
+        lat.update(e, r)
+        post = oracle.update(0, n, 1, post, _rev(e, n), r, in_place=True)
+    _assert_lookahead(oracle, post, n, lat.select_experiments(c["count"]), c["experiments"])

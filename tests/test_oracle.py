@@ -204,3 +204,14 @@ def test_lookahead_bit_exact_against_reference(oracle):
         for e, r in updates:
             post = oracle.update(0, n, 1, post, _rev(e, n), r, in_place=True)
         assert oracle.select_experiments(post, n, count) == ref.select_experiments(pi0, updates, count), (n, updates)
+
+
+@pytest.mark.parametrize("case", range(len(GOLDEN.get("lookahead", []))))
+def test_golden_lookahead(oracle, case):
+    # select_experiments outputs of the reference library (tests/golden/make_golden.py).
+    c = GOLDEN["lookahead"][case]
+    n = c["n"]
+    post = oracle.prior(c["pi0"])
+    for e, r in c["updates"]:
+        post = oracle.update(0, n, 1, post, _rev(e, n), r, in_place=True)
+    assert oracle.select_experiments(post, n, c["count"]) == c["experiments"]
