@@ -1180,6 +1180,17 @@ inline bool log_enabled(LogLevel level, LogSubsystem subsystem)
 	return false;
 }
 
+// Device-memory budget of lattice handles (bgt_gpu_set_memory_limit): an
+// allocation past it throws Error(cuda_error) before the device is asked;
+// 0 removes the limit.
+inline void set_memory_limit(std::uint64_t bytes) { detail::check(bgt_gpu_set_memory_limit(bytes)); }
+inline std::uint64_t memory_in_use()
+{
+	uint64_t bytes = 0;
+	detail::check(bgt_gpu_memory_in_use(&bytes));
+	return bytes;
+}
+
 // The CPU provider is always available, as in the reference; this package
 // runs only the device path.
 inline std::vector<Provider> available_providers()

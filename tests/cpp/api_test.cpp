@@ -204,6 +204,17 @@ int main(int argc, char **argv)
 		bgt::set_log_config(bgt::LogConfig{});
 	}
 
+	{
+		// Allocation failure through the lattice budget: an Error, nothing leaked.
+		const std::uint64_t used = bgt::memory_in_use();
+		bgt::set_memory_limit(used + 4096);
+		expect_error([&] { bgt::Lattice big(bgt::LatticeType::replicated_non_dilution, 18, std::vector<double>(18, 0.05)); },
+					 bgt::StatusCode::cuda_error, "lattice over the memory budget");
+		bgt::set_memory_limit(0);
+		expect_equal(static_cast<long long>(bgt::memory_in_use()), static_cast<long long>(used),
+					 "failed create released its memory");
+	}
+
 	const std::vector<double> multinomial_prior{0.11, 0.23, 0.31, 0.41, 0.17, 0.29};
 	bgt::Lattice multinomial(bgt::LatticeType::replicated_non_dilution, 3, 2, multinomial_prior);
 	expect_equal(multinomial.select_experiment(bgt::SelectorType::op_bbpa), brute_force_bbpa(multinomial, 3, 2),
