@@ -54,3 +54,22 @@ def test_single_rank_is_unchanged():
     assert bench.max_over_ranks([1.5, 2.5], 1) == [1.5, 2.5]
     assert bench.replica_throughput(3200, 1, 0.5) == pytest.approx(6400.0)
     assert bench.rank_session(0, 7) == 7 and bench.rank_session(1, 0) == 1 << 32
+
+
+def test_reference_arm_under_two_ranks():
+    # `bench.py --impl reference` launched as two ranks: rank 0 alone times the
+    # CPU implementation and prints the one JSON line; rank 1 exits 0.
+    import json
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference",
+           "--steps", "1", "--warmup", "0", "--gpus", "2"]
+    out = subprocess.run(cmd, cwd=repo, capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(l) for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = lines[0]
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
