@@ -334,7 +334,7 @@ void upload_block_lists(const LatticeGeometry &g, unsigned int **blocks, unsigne
 			   "column-block list up");
 }
 
-// Validates a request against what this build supports; returns 0 or a status.
+// Validates a request against what the library supports; returns 0 or a status.
 int check_supported(int subjects, int variants, int dilution, std::string *why)
 {
 	if (subjects <= 0 || variants <= 0)
@@ -356,7 +356,8 @@ int check_supported(int subjects, int variants, int dilution, std::string *why)
 			entries *= dilution ? subjects + 1 : 2;
 			if (entries > kMaxClassTable)
 			{
-				*why = "too many multinomial likelihood classes for this build";
+				*why = "too many multinomial likelihood classes (the class table holds " +
+					   std::to_string(kMaxClassTable) + ")";
 				return BGT_GPU_UNSUPPORTED;
 			}
 		}
