@@ -333,6 +333,21 @@ class SimulationTimings:
 
 
 @dataclass
+class ProgressSnapshot:
+    """bgt::ProgressSnapshot (include/bgt/simulation.hpp:74-85): one progress record."""
+
+    status: SimulationRunStatus = SimulationRunStatus.completed
+    reason: TerminationReason = TerminationReason.none
+    total_states: int = 0
+    evaluated_states: int = 0
+    state_coverage_fraction: float = 0.0
+    evaluated_prior_mass: float = 0.0
+    stats: TreeStats = field(default_factory=TreeStats)
+    timings: SimulationTimings = field(default_factory=SimulationTimings)
+    message: str = ""
+
+
+@dataclass
 class TestAccuracy:
     """Non-dilution test accuracy, an extension: the reference fixes both at
     0.99 (src/core/model/replicated_lattice.cpp:6-14).  P(negative response |

@@ -15,8 +15,8 @@ import os
 import sys
 import time
 
-from .api import (SimulationConfig, SimulationMode, SimulationResult, SimulationRunStatus, SimulationTimings,
-                  TerminationReason, TreeStats, simulation_cancellation_reason)
+from .api import (ProgressSnapshot, SimulationConfig, SimulationMode, SimulationResult, SimulationRunStatus,
+                  SimulationTimings, TerminationReason, TreeStats, simulation_cancellation_reason)
 
 
 def simulation_mode_name(mode: SimulationMode) -> str:
@@ -160,11 +160,19 @@ class ProgressTracker:
         if self.stats.total_leaves == 0:
             self.stats.total_leaves = known
 
-    def _snapshot(self, status: SimulationRunStatus, reason: TerminationReason, message: str):
+    def snapshot(self, status: SimulationRunStatus, reason: TerminationReason, message: str) -> ProgressSnapshot:
+        """The record the tracker writes now (ProgressTracker::snapshot,
+        src/runtime/progress.cpp:217-261)."""
         timings = SimulationTimings(self.timings.setup_seconds, self.timings.tree_build_seconds,
                                     self.timings.evaluation_seconds, time.perf_counter() - self.total_start)
-        return snapshot_json(status, reason, self.total_states, self.evaluated_states, self.evaluated_prior_mass,
-                             self.stats, timings, message), timings.total_seconds
+        coverage = 0.0 if self.total_states == 0 else self.evaluated_states / self.total_states
+        return ProgressSnapshot(status, reason, self.total_states, self.evaluated_states, coverage,
+                                self.evaluated_prior_mass, self.stats, timings, message)
+
+    def _snapshot(self, status: SimulationRunStatus, reason: TerminationReason, message: str):
+        snap = self.snapshot(status, reason, message)
+        return snapshot_json(snap.status, snap.reason, snap.total_states, snap.evaluated_states,
+                             snap.evaluated_prior_mass, snap.stats, snap.timings, snap.message), snap.timings.total_seconds
 
     def maybe_emit(self, message: str, force: bool = False) -> bool:
         if not self._enabled():

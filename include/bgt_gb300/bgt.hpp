@@ -449,6 +449,20 @@ struct ProgressConfig
 // reference's CUDA path, evaluation_prior, true_state_policy, trim_percent,
 // global_tree_depth and workload_granularity do not change a local_tree run on
 // the device (every true state is evaluated under the prior).
+// bgt::ProgressSnapshot (include/bgt/simulation.hpp:74-85): one progress record.
+struct ProgressSnapshot
+{
+	SimulationRunStatus status = SimulationRunStatus::completed;
+	TerminationReason reason = TerminationReason::none;
+	int total_states = 0;
+	int evaluated_states = 0;
+	double state_coverage_fraction = 0.0;
+	host_probability_t evaluated_prior_mass = 0.0;
+	TreeStats stats;
+	SimulationTimings timings;
+	std::string message;
+};
+
 // Non-dilution test accuracy, an extension: the reference fixes both at 0.99
 // (src/core/model/replicated_lattice.cpp:6-14).  P(negative response | no
 // pooled positive) = specificity, P(positive response | a pooled positive) =
@@ -769,24 +783,45 @@ class ProgressTracker
 		return config_.report.output_directory / (run_name(config_) + ".progress.json");
 	}
 
+  public:
+	// The record the tracker writes now (ProgressTracker::snapshot,
+	// src/runtime/progress.cpp:217-261).
+	ProgressSnapshot snapshot(SimulationRunStatus status, TerminationReason reason, const std::string &message) const
+	{
+		ProgressSnapshot snap;
+		snap.status = status;
+		snap.reason = reason;
+		snap.total_states = total_states_;
+		snap.evaluated_states = evaluated_;
+		snap.state_coverage_fraction =
+			total_states_ == 0 ? 0.0 : static_cast<double>(evaluated_) / static_cast<double>(total_states_);
+		snap.evaluated_prior_mass = prior_mass_;
+		snap.stats = stats_;
+		snap.timings.total_seconds = seconds_since(start_);
+		snap.message = message;
+		return snap;
+	}
+
+  private:
 	void write(SimulationRunStatus status, TerminationReason reason, const std::string &message) const
 	{
-		const double elapsed = seconds_since(start_);
-		const double coverage =
-			total_states_ == 0 ? 0.0 : static_cast<double>(evaluated_) / static_cast<double>(total_states_);
+		const ProgressSnapshot snap = snapshot(status, reason, message);
+		const double elapsed = snap.timings.total_seconds;
+		const double coverage = snap.state_coverage_fraction;
+		const TreeStats &st = snap.stats;
 		std::ostringstream body;
-		body << std::setprecision(17) << "{\"status\":\"" << status_name(status) << "\",\"termination_reason\":\""
-			 << reason_name(reason) << "\",\"total_states\":" << total_states_ << ",\"evaluated_states\":" << evaluated_
-			 << ",\"state_coverage_fraction\":" << coverage << ",\"evaluated_prior_mass\":" << prior_mass_
-			 << ",\"stats\":{\"total_leaves\":" << stats_.total_leaves
-			 << ",\"correct_probability\":" << stats_.correct_probability
-			 << ",\"incorrect_probability\":" << stats_.incorrect_probability
-			 << ",\"false_positive_probability\":" << stats_.false_positive_probability
-			 << ",\"false_negative_probability\":" << stats_.false_negative_probability
-			 << ",\"unclassified_probability\":" << stats_.unclassified_probability
-			 << ",\"expected_stages\":" << stats_.expected_stages << ",\"expected_tests\":" << stats_.expected_tests
+		body << std::setprecision(17) << "{\"status\":\"" << status_name(snap.status)
+			 << "\",\"termination_reason\":\"" << reason_name(snap.reason) << "\",\"total_states\":" << snap.total_states
+			 << ",\"evaluated_states\":" << snap.evaluated_states << ",\"state_coverage_fraction\":" << coverage
+			 << ",\"evaluated_prior_mass\":" << snap.evaluated_prior_mass << ",\"stats\":{\"total_leaves\":" << st.total_leaves
+			 << ",\"correct_probability\":" << st.correct_probability
+			 << ",\"incorrect_probability\":" << st.incorrect_probability
+			 << ",\"false_positive_probability\":" << st.false_positive_probability
+			 << ",\"false_negative_probability\":" << st.false_negative_probability
+			 << ",\"unclassified_probability\":" << st.unclassified_probability
+			 << ",\"expected_stages\":" << st.expected_stages << ",\"expected_tests\":" << st.expected_tests
 			 << "},\"timings\":{\"setup_seconds\":0,\"tree_build_seconds\":0,\"evaluation_seconds\":0,"
-			 << "\"total_seconds\":" << elapsed << "},\"message\":\"" << json_escape(message) << "\"}";
+			 << "\"total_seconds\":" << elapsed << "},\"message\":\"" << json_escape(snap.message) << "\"}";
 		const std::filesystem::path latest = latest_path();
 		if (!latest.parent_path().empty())
 			std::filesystem::create_directories(latest.parent_path());

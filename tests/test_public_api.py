@@ -124,3 +124,25 @@ def test_kernel_specs():
     assert bgt.Runtime().make_kernel_spec(binary).selector == bgt.SelectorType.op_bha
     multi = bgt.SimulationConfig(subjects=1, variants=2, prior=[0.2, 0.4])
     assert bgt.Runtime().make_kernel_spec(multi).selector == bgt.SelectorType.op_bbpa
+
+
+def test_progress_snapshot(tmp_path):
+    snap = bgt.ProgressSnapshot()
+    assert snap.status == bgt.SimulationRunStatus.completed and snap.reason == bgt.TerminationReason.none
+    assert snap.total_states == 0 and snap.evaluated_states == 0 and snap.message == ""
+    # the tracker's snapshot is the record it writes
+    import json
+    import time
+    from bayesiangrouptesting_gb300.reporting import ProgressTracker
+    cfg = bgt.SimulationConfig(subjects=2, prior=[0.2, 0.4])
+    cfg.progress.enabled = True
+    cfg.progress.output_path = str(tmp_path / "p.json")
+    tracker = ProgressTracker(cfg, 0, 4, time.perf_counter())
+    tracker.replace_state(4, 1.0, bgt.TreeStats(total_leaves=3, correct_probability=0.5))
+    snap = tracker.snapshot(bgt.SimulationRunStatus.completed, bgt.TerminationReason.none, "done")
+    assert (snap.total_states, snap.evaluated_states, snap.state_coverage_fraction) == (4, 4, 1.0)
+    assert snap.stats.total_leaves == 3 and snap.message == "done"
+    tracker.finish(bgt.SimulationRunStatus.completed, bgt.TerminationReason.none, "done")
+    rec = json.loads((tmp_path / "p.json").read_text())
+    assert rec["evaluated_states"] == 4 and rec["stats"]["total_leaves"] == 3 and rec["message"] == "done"
+    assert rec["status"] == "completed"
