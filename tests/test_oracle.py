@@ -215,3 +215,23 @@ def test_golden_lookahead(oracle, case):
     for e, r in c["updates"]:
         post = oracle.update(0, n, 1, post, _rev(e, n), r, in_place=True)
     assert oracle.select_experiments(post, n, c["count"]) == c["experiments"]
+
+
+def test_session_sampler_test_accuracy(oracle):
+    # bgt_session_sample_response (include/bgt_session_rng.h) under a
+    # non-dilution accuracy: bit v set (negative) when the stream's uniform
+    # is below specificity for a contained pool, below 1 - sensitivity else.
+    rng = np.random.default_rng(12)
+    for sens, spec in ((0.95, 0.98), (0.99, 0.99), (0.7, 0.6)):
+        with oracle.test_accuracy(sens, spec):
+            for t in range(200):
+                n, k = int(rng.integers(1, 8)), int(rng.integers(1, 4))
+                e = int(rng.integers(1, 1 << n))
+                s = int(rng.integers(0, 1 << (n * k)))
+                want = 0
+                for v in range(k):
+                    sv = (s >> (v * n)) & ((1 << n) - 1)
+                    p1 = spec if (e & sv) == e else 1.0 - sens
+                    if oracle.lib.orc_uniform(9, t, 3, (t % 40) * 64 + v) < p1:
+                        want |= 1 << v
+                assert oracle.lib.orc_sample_response(0, n, k, e, s, 0.99, 0.005, 9, t, t % 40) == want
