@@ -158,7 +158,11 @@ def log_message(level: LogLevel, subsystem: LogSubsystem, message: str) -> None:
     and line go into the prefix)."""
     if not log_enabled(level, subsystem):
         return
-    caller = inspect.stack()[1]
+    frame = inspect.currentframe()
+    caller = frame.f_back if frame is not None and frame.f_back is not None else None
+    filename = caller.f_code.co_filename if caller is not None else "?"
+    lineno = caller.f_lineno if caller is not None else 0
+    del frame, caller
     with _lock:
         cfg = copy.deepcopy(_config)
     parts = []
@@ -168,7 +172,7 @@ def log_message(level: LogLevel, subsystem: LogSubsystem, message: str) -> None:
     rank = _rank()
     if rank is not None:
         parts.append(f"rank={rank[0]}/{rank[1]}")
-    parts.append(f"{os.path.basename(caller.filename)}:{caller.lineno}: {message}")
+    parts.append(f"{os.path.basename(filename)}:{lineno}: {message}")
     line = " ".join(parts)
     if cfg.color and not cfg.file_path:
         colour = {LogLevel.fatal: 31, LogLevel.error: 31, LogLevel.warn: 33, LogLevel.info: 32}.get(level, 36)
